@@ -1,0 +1,358 @@
+"""Benchmark of the PT Metropolis hot path (one JSON line on rank 0).
+
+Workload (default): dense integer QUBO, N=1024, Q_ij uniform in [-8, 8]
+symmetric, diagonal uniform in [-16, 16], float32; 64 replicas on a geometric
+ladder T = 0.5 .. 8.0; 256 reads (16384 chains); sequential sweeps with a
+replica exchange after every sweep.  Seeded synthetic instance.
+
+A step is one sweep of every chain followed by the exchange.  `value` is
+spin-flip attempts/s with all state resident in HBM, timed on the device with
+CUDA events around each step; L2 is flushed (256 MB write) before every step.
+`e2e` is the same metric through the public API (Solver.metropolis_update,
+2000 sweeps) with host inputs and outputs, timed on the host.
+
+--impl reference times the CPU restatement of the reference's algorithm
+(dense dot per attempt, OpenMP over chains) on the same instance.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "qubo1024": dict(kind="qubo", n=1024, replicas=64, reads=256, tmin=0.5,
+                     tmax=8.0, sweeps=2000, update="sequential"),
+    "qubo1024_random": dict(kind="qubo", n=1024, replicas=64, reads=256,
+                            tmin=0.5, tmax=8.0, sweeps=2000, update="random"),
+    "sk128": dict(kind="sk", n=128, replicas=32, reads=100, tmin=1.0,
+                  tmax=3.5, sweeps=1000, update="sequential"),
+}
+
+
+def make_instance(w: dict, seed: int = 2024):
+    rng = np.random.default_rng(seed)
+    n = w["n"]
+    if w["kind"] == "qubo":
+        Q = rng.integers(-8, 9, (n, n))
+        Q = np.triu(Q, 1)
+        Q = Q + Q.T
+        Q[np.diag_indices(n)] = rng.integers(-16, 17, n)
+        return "qubo", Q.astype(np.float32)
+    J = np.triu(rng.normal(size=(n, n)) / np.sqrt(n), 1)
+    return "ising", (J + J.T).astype(np.float32)
+
+
+def ladder(w):
+    R = w["replicas"]
+    ratio = np.exp(1 / (R - 1) * np.log(w["tmax"] / w["tmin"]))
+    return np.array([1 / (w["tmin"] * ratio**k) for k in range(R)],
+                    np.float32)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_reference(w, ptype, P, reads, sweeps, nthreads=0):
+    """Oracle (CPU restatement, OpenMP over chains) on `reads` reads."""
+    from oracle import oracle
+    oracle.build()
+    h = np.diag(P).astype(np.float32).copy()
+    J = P.copy()
+    np.fill_diagonal(J, 0)
+    R, n = w["replicas"], w["n"]
+    rng = np.random.default_rng(5)
+    if ptype == "qubo":
+        x0 = rng.integers(0, 2, (reads, R, n)).astype(np.float32)
+    else:
+        x0 = (2 * rng.integers(0, 2, (reads, R, n)) - 1).astype(np.float32)
+    e0 = np.zeros((reads, R), np.float32)
+    bidx = np.tile(np.arange(R, dtype=np.int32), (reads, 1))
+    t0 = time.perf_counter()
+    oracle.pt_run(ptype, J, h, ladder(w), x0, e0, bidx, seed=1,
+                  num_sweeps=sweeps, update=w["update"], nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return reads * R * n * sweeps / dt, dt
+
+
+def run_reference_arm(args, w, rank, world):
+    if rank != 0:
+        return 0
+    ptype, P = make_instance(w)
+    cores = os.cpu_count() or 1
+    reads = 4  # bounded sample: 4 reads x all replicas x 1 sweep per step
+    for _ in range(args.warmup):
+        cpu_reference(w, ptype, P, reads, 1)
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, dt = cpu_reference(w, ptype, P, reads, 1)
+        rates.append(r)
+        times.append(dt)
+    total_attempts = reads * w["replicas"] * w["n"] * args.steps
+    value = total_attempts / sum(times)
+    line = {
+        "impl": "reference", "metric": "spin_flip_attempts_per_s",
+        "value": value, "unit": "attempts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, **{k: w[k] for k in w}},
+        "cpu_baseline": {
+            "value": value, "unit": "attempts/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{reads} reads x {w['replicas']} replicas x 1 sweep per "
+                      "step; C restatement of the reference's dense-dot rule, "
+                      "OpenMP over chains (numba not available)"},
+        "e2e": {"value": value, "unit": "attempts/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="qubo1024", choices=list(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-sweeps", type=int, default=None)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference_arm(args, w, rank, world)
+
+    import torch
+    from pysa_gb300 import Instance, PTBatch, Solver, pack_spins
+    from pysa_gb300 import _lib
+    from pysa_gb300._lib import check, ref
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ptype, P = make_instance(w)
+    h = np.diag(P).astype(np.float32).copy()
+    J = P.copy()
+    np.fill_diagonal(J, 0)
+    R, Rd, n = w["replicas"], w["reads"], w["n"]
+    batch = PTBatch(ptype, [Instance(J, h, ladder(w), Rd)])
+    rng = np.random.default_rng(100 + rank)
+    if ptype == "qubo":
+        x0 = rng.integers(0, 2, (Rd, R, n)).astype(np.float32)
+    else:
+        x0 = (2 * rng.integers(0, 2, (Rd, R, n)) - 1).astype(np.float32)
+    batch.set_states(pack_spins(x0, ptype, batch.words), None)
+    upd = _lib.RANDOM if w["update"] == "random" else _lib.SEQUENTIAL
+    seed = 7 + rank
+
+    def opts(phases):
+        return _lib.Options(seed, upd, 1, 0, 0, phases, 0)
+
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+    lib = batch.lib
+    o_all, o_sweep, o_x = opts(3), opts(1), opts(2)
+    check(lib.pysa_gb_sweeps(ref(batch.p), ref(batch.s), ref(batch.ws),
+                             ref(o_all), 0, st), "sweeps")
+    for _ in range(args.warmup):
+        check(lib.pysa_gb_sweeps(ref(batch.p), ref(batch.s), ref(batch.ws),
+                                 ref(o_all), 1, st), "sweeps")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    with sampler:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(float(k))  # L2 flush (256 MB > 129 MB L2), untimed
+            a, b, c = ev[k]
+            a.record(stream)
+            check(lib.pysa_gb_sweeps(ref(batch.p), ref(batch.s), ref(batch.ws),
+                                     ref(o_sweep), 1, st), "sweep")
+            b.record(stream)
+            check(lib.pysa_gb_sweeps(ref(batch.p), ref(batch.s), ref(batch.ws),
+                                     ref(o_x), 1, st), "exchange")
+            c.record(stream)
+        torch.cuda.synchronize()
+    batch.check_status()
+    sweep_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    step_ms = [a.elapsed_time(c) for a, _, c in ev]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    attempts_per_step = Rd * R * n
+    value = attempts_per_step * args.steps * world / total_s
+
+    # roofline of the sweep kernel: algorithmic bytes of one launch =
+    # fields read+write + spins read+write + J once
+    C = Rd * R
+    alg_bytes = C * (2 * 4 * n + 2 * 4 * batch.words + 16) + 4 * n * n
+    sweep_s = np.mean(sweep_ms) / 1e3
+    hbm, bf16, peak_kind = measured_peaks()
+    achieved = alg_bytes / sweep_s / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "sweep_plain_qubo1024_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+
+    # end to end through the public API (host buffers in and out)
+    e2e = None
+    if not args.no_e2e:
+        sweeps_e2e = args.e2e_sweeps or w["sweeps"]
+        solver = Solver(P.astype(np.float64), ptype, "float32")
+        kw = dict(num_sweeps=sweeps_e2e, num_reads=Rd, num_replicas=R,
+                  min_temp=w["tmin"], max_temp=w["tmax"],
+                  update_strategy=w["update"], return_dataframe=False)
+        np.random.seed(rank)
+        solver.metropolis_update(**dict(kw, num_sweeps=2), seed=1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rows = solver.metropolis_update(**kw, seed=2)
+        e2e_s = time.perf_counter() - t0
+        words = batch.words
+        h2d = 4 * n * n + 4 * n + 4 * R + C * words * 4 + C * 4
+        d2h = C * (words * 4 * 2 + 4 * 4)
+        e2e = {"value": Rd * R * n * sweeps_e2e / e2e_s, "unit": "attempts/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "sweeps_per_call": sweeps_e2e, "seconds": e2e_s,
+               "best_energy_min": float(min(r["best_energy"] for r in rows))}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        reads_cpu = 8
+        sweeps_cpu = 5
+        rate, dt = cpu_reference(w, ptype, P, reads_cpu, sweeps_cpu)
+        cpu = {"value": rate, "unit": "attempts/s",
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{reads_cpu} reads x {R} replicas x {sweeps_cpu} "
+                         f"sweeps of the same instance ({dt:.1f} s); C "
+                         "restatement of the reference's dense-dot update, "
+                         "OpenMP over chains"}
+
+    if rank == 0:
+        line = {
+            "metric": "spin_flip_attempts_per_s", "value": value,
+            "unit": "attempts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "n": n, "replicas": R,
+                       "reads": Rd, "chains": C, "update": w["update"],
+                       "exchange": "every sweep", "problem": w["kind"],
+                       "l2": "flushed (256 MB write) before every step",
+                       "kernel": "plain local-field sweep (CUDA cores)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_sweep_plain<32,4,8,8>",
+                         "sweep_ms": float(np.mean(sweep_ms)),
+                         "alg_bytes_per_launch": int(alg_bytes)},
+            "clocks": sampler.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": 2 * args.steps + (args.steps if upd else 0),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,224 @@
+/*
+ * pysa_gb.h -- C ABI of the GB300 parallel-tempering simulated-annealing core.
+ *
+ * Drop-in boundary for the hot path of nasa/PySA: the driver call
+ *     simulation(update_spin, sweep, couplings, local_fields, states,
+ *                energies, beta_idx, betas, n_sweeps, get_part_fun, use_pt)
+ * made by pysa/sa.py:329-332 and pysa/sa.py:349-352 (drivers
+ * pysa/simulation.py:123-236, update rules pysa/ising.py:40-63 and
+ * pysa/qubo.py:40-63, exchange pysa/utils.py:26-58), the energy function
+ * pysa/ising.py:32-37, and the AIS sampler of pysa/sa.py:432-553
+ * (pysa/simulation.py:239-317, pysa/ais.py:79-131).
+ *
+ * Conventions
+ *   - Every pointer in the structs below is DEVICE memory owned by the caller;
+ *     the library allocates nothing and keeps no per-call state.
+ *   - All work is enqueued on the given cudaStream_t (passed as void*);
+ *     entry points return immediately.  They are reentrant per stream.
+ *   - Return value: 0 on success, a negative PYSA_GB_ERR_* code otherwise;
+ *     pysa_gb_last_error() returns a message for the calling thread.
+ *     Device-side failures (a bounded wait that ran out) are reported in the
+ *     caller's status word, read after the stream synchronises.
+ *   - Spins are bit-packed: bit (j % 32) of word (j / 32) of a chain holds
+ *     spin j; 1 means +1 (Ising) or 1 (QUBO), 0 means -1 (Ising) or 0 (QUBO).
+ *   - A chain is one replica of one read of one instance; the chains of an
+ *     instance are numbered read-major (read * R + replica) from
+ *     chain_off[instance].
+ */
+#ifndef PYSA_GB_H
+#define PYSA_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYSA_GB_ABI_VERSION 1
+
+enum {
+  PYSA_GB_ISING = 0,
+  PYSA_GB_QUBO = 1
+};
+
+enum {
+  PYSA_GB_SEQUENTIAL = 0, /* sequential_sweep, pysa/simulation.py:60-76 */
+  PYSA_GB_RANDOM = 1      /* random_sweep, pysa/simulation.py:41-57 */
+};
+
+enum {
+  PYSA_GB_OK = 0,
+  PYSA_GB_ERR_ARG = -1,     /* invalid argument */
+  PYSA_GB_ERR_SIZE = -2,    /* size beyond what the kernels support */
+  PYSA_GB_ERR_CUDA = -3,    /* a CUDA runtime call failed */
+  PYSA_GB_ERR_TIMEOUT = -4, /* (status word) a bounded device wait ran out */
+  PYSA_GB_ERR_NOBETA0 = -5  /* log-omega requested without a beta = 0 slot */
+};
+
+/* Largest number of spins per instance the sweep kernels accept. */
+#define PYSA_GB_MAX_N 4096
+
+/* A batch of dense problems (one or many instances, uneven sizes allowed). */
+typedef struct {
+  int32_t problem_type;   /* PYSA_GB_ISING or PYSA_GB_QUBO */
+  int32_t num_instances;
+  int32_t max_n;          /* largest n over the instances */
+  int32_t words;          /* spin words per chain = ceil(max_n / 32) */
+  int64_t num_chains;     /* sum over instances of reads * replicas */
+  int64_t num_reads;      /* sum over instances of reads */
+  /* per-instance tables [num_instances] */
+  const int32_t *n;         /* spins */
+  const int32_t *replicas;  /* R */
+  const int32_t *reads;     /* Rd */
+  const int64_t *j_off;     /* element offset of J (n x ld, f32, row-major) */
+  const int32_t *ld;        /* row stride of J, >= n, multiple of 4 */
+  const int64_t *h_off;     /* element offset of h (n entries) */
+  const int64_t *chain_off; /* first chain of the instance */
+  const int64_t *read_off;  /* first read of the instance */
+  const int64_t *ladder_off;/* offset of the instance's R betas (slot order) */
+  /* per-read table [num_reads] */
+  const int32_t *read_inst; /* instance of each read */
+  /* data */
+  const float *J;           /* couplings with zero diagonal (pysa/sa.py:67-70),
+                               stored TRANSPOSED: row j of this buffer is
+                               column j of the coupling matrix, i.e. the
+                               field change when spin j flips (the same
+                               thing for the symmetric problems accepted by
+                               pysa/sa.py:64-65 up to allclose tolerance) */
+  const float *h;           /* local fields = diagonal of the problem */
+  const float *ladder;      /* inverse temperatures, slot order */
+  const int32_t *ladder_sorted; /* per instance: argsort of its R betas */
+} pysa_gb_problems;
+
+/* Chain state, updated in place by the sweeps. */
+typedef struct {
+  uint32_t *spins;        /* [num_chains, words] */
+  float *energies;        /* [num_chains] accumulated energies */
+  int32_t *beta_idx;      /* [num_chains]: per read, slot k -> replica */
+  float *chain_beta;      /* [num_chains] beta each chain runs at */
+  float *best_energy;     /* [num_chains] lowest energy seen (strict <) */
+  int32_t *best_sweep;    /* [num_chains] sweep index of best_energy */
+  uint32_t *best_spins;   /* [num_chains, words] state at best_energy */
+  double *log_omega;      /* [num_reads, log_omega_stride] or NULL */
+  int64_t *sweep_counter; /* [1] index of the next sweep */
+  int32_t *status;        /* [1] 0 or a PYSA_GB_ERR_* code from the device */
+  uint32_t *ticket;       /* [1] zero-initialised scratch word */
+} pysa_gb_state;
+
+/* Per-call workspace, caller-allocated (sizes from pysa_gb_workspace_bytes). */
+typedef struct {
+  float *fields;          /* local fields, [num_chains, field_ld] */
+  int32_t field_ld;       /* row stride of fields (>= 32 * ceil(max_n/32)) */
+  int32_t perm_slots;     /* visiting orders held (sweeps per batch) */
+  int32_t *perm;          /* [perm_slots, num_instances, max_n] */
+  float *packed_j;        /* couplings in the sweep kernel's row layout */
+  int64_t packed_j_elems; /* capacity of packed_j */
+  int32_t *items;         /* [num_items, 8] work list of the sweep kernel */
+  int32_t num_items;      /* capacity of items, in work items */
+  int32_t variant_start[8]; /* host: first work item of each kernel variant */
+  int32_t variant_count[8]; /* host: work items of each kernel variant */
+} pysa_gb_workspace;
+
+/* Host copies of the per-instance tables, used to plan the work list. */
+typedef struct {
+  const int32_t *n;
+  const int32_t *replicas;
+  const int32_t *reads;
+  const int64_t *chain_off;
+  const int64_t *j_off;
+  const int32_t *ld;
+} pysa_gb_host_tables;
+
+typedef struct {
+  uint64_t seed;           /* key of the Philox stream */
+  int32_t update;          /* PYSA_GB_SEQUENTIAL or PYSA_GB_RANDOM */
+  int32_t use_pt;          /* 1: replica exchange after every sweep */
+  int32_t log_omega_stride;/* 0: off; else row stride of state.log_omega */
+  int32_t best_global;     /* 0: per-replica best (simulation_parallel);
+                              1: energies start at +inf best (sequential) */
+  int32_t phases;          /* 0 = all; bit 0: visiting order + sweep kernel,
+                              bit 1: exchange (lets a caller time each) */
+  int32_t pad_;
+} pysa_gb_options;
+
+/* ABI version (PYSA_GB_ABI_VERSION) and the last error of this thread. */
+int pysa_gb_abi_version(void);
+const char *pysa_gb_last_error(void);
+
+/* Workspace sizing and set-up.
+ *   pysa_gb_workspace_bytes: sizes of the workspace arrays for a batch
+ *     described by host tables (n, replicas, reads are read); returns the
+ *     number of work items (>= 0) or an error.  out[0] packed_j elements,
+ *     out[1] items int32 entries, out[2] minimum field_ld.
+ *   pysa_gb_setup: packs J into the sweep kernel's row layout and writes the
+ *     work list; fills ws->variant_start / variant_count. */
+int pysa_gb_workspace_bytes(int32_t num_instances,
+                            const pysa_gb_host_tables *host, int64_t out[3]);
+int pysa_gb_setup(const pysa_gb_problems *p, const pysa_gb_host_tables *host,
+                  pysa_gb_workspace *ws, void *stream);
+
+/* Local fields H = J s + h for every chain, accumulated in f64 from f32
+ * products, and (if set_energies) energies E = s.(J s / 2 + h)
+ * (pysa/ising.py:32-37, pysa/qubo.py:32-37).  Also sets chain_beta from
+ * beta_idx and, if init_best, best_* from the current state
+ * (best_global: best_energy = +inf). */
+int pysa_gb_prepare(const pysa_gb_problems *p, pysa_gb_state *s,
+                    pysa_gb_workspace *ws, int32_t set_energies,
+                    int32_t init_best, int32_t best_global, void *stream);
+
+/* num_sweeps Metropolis sweeps, each followed by the replica exchange
+ * (pysa/utils.py:44-58) and, when enabled, the log-omega of the sorted ladder
+ * (pysa/ais.py:79-112).  Replaces the loop of simulation_parallel
+ * (pysa/simulation.py:150-171).  Sweep indices come from
+ * state.sweep_counter, so the same enqueued work can be replayed by a CUDA
+ * graph. */
+int pysa_gb_sweeps(const pysa_gb_problems *p, pysa_gb_state *s,
+                   pysa_gb_workspace *ws, const pysa_gb_options *o,
+                   int32_t num_sweeps, void *stream);
+
+/* Energies in f64 of `count` bit-packed states of instance `inst`
+ * (get_energy, pysa/ising.py:32-37) with f64 couplings J64 (n x ld64). */
+int pysa_gb_energy64(int32_t problem_type, int32_t n, int32_t ld64,
+                     const double *J64, const double *h64,
+                     const uint32_t *spins, int32_t words, int64_t count,
+                     double *out, void *stream);
+
+/* Unpack bit-packed spins into float32 values (+-1 or 0/1), [count, n]. */
+int pysa_gb_unpack(int32_t problem_type, int32_t n, const uint32_t *spins,
+                   int32_t words, int64_t count, float *out, int32_t out_ld,
+                   void *stream);
+
+/* Annealed importance sampling (Solver.annealed_importance, pysa/sa.py:432-553;
+ * ais_sample, pysa/simulation.py:293-317; update_spin_ref,
+ * pysa/ising.py:66-92).  One instance; state.spins holds the initial samples
+ * [samples, words], state.energies their energies and ws.fields their local
+ * fields (from pysa_gb_prepare, with the couplings already scaled by the
+ * target beta).  Writes final samples, energies and the f64 log weights. */
+typedef struct {
+  uint64_t seed;
+  int32_t update;     /* PYSA_GB_SEQUENTIAL or PYSA_GB_RANDOM */
+  int32_t reference;  /* 0 uniform (pysa/ais.py:137-169),
+                         1 bernoulli (pysa/ais.py:175-226) */
+  int32_t order;      /* 0: weight after each sweep (pysa/simulation.py:305-316);
+                         1: weight before each sweep (standard AIS) */
+  int32_t num_temps;
+  double p;           /* bernoulli: probability of bit 0 / spin -1 */
+} pysa_gb_ais_options;
+
+int pysa_gb_ais(const pysa_gb_problems *p, pysa_gb_state *s,
+                pysa_gb_workspace *ws, const pysa_gb_ais_options *o,
+                const float *temps, double *log_w, void *stream);
+
+/* Exact log Z(beta) = log sum_s exp(-beta E(s)) of every instance by
+ * enumeration of all 2^n states in f64 (n <= 34).  part_max / part_sum are
+ * caller buffers of pysa_gb_logz_parts(...) doubles each; the host combines
+ * them: logZ = M + log(sum_b part_sum[b] exp(part_max[b] - M)). */
+int64_t pysa_gb_logz_parts(int32_t num_instances, int32_t max_n);
+int pysa_gb_logz_exact(const pysa_gb_problems *p, double beta,
+                       double *part_max, double *part_sum, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYSA_GB_H */

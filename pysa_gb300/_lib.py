@@ -1,0 +1,109 @@
+"""ctypes binding of libpysa_gb.so (the C ABI in include/pysa_gb.h).
+
+The structures below mirror the header field for field.  Loading fails
+loudly when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpysa_gb.so")
+
+ISING, QUBO = 0, 1
+SEQUENTIAL, RANDOM = 0, 1
+ERR_TIMEOUT = -4
+
+P = ctypes.c_void_p
+I32, I64, U64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64
+
+
+class Problems(ctypes.Structure):
+    _fields_ = [("problem_type", I32), ("num_instances", I32), ("max_n", I32),
+                ("words", I32), ("num_chains", I64), ("num_reads", I64),
+                ("n", P), ("replicas", P), ("reads", P), ("j_off", P),
+                ("ld", P), ("h_off", P), ("chain_off", P), ("read_off", P),
+                ("ladder_off", P), ("read_inst", P), ("J", P), ("h", P),
+                ("ladder", P), ("ladder_sorted", P)]
+
+
+class State(ctypes.Structure):
+    _fields_ = [("spins", P), ("energies", P), ("beta_idx", P),
+                ("chain_beta", P), ("best_energy", P), ("best_sweep", P),
+                ("best_spins", P), ("log_omega", P), ("sweep_counter", P),
+                ("status", P), ("ticket", P)]
+
+
+class Workspace(ctypes.Structure):
+    _fields_ = [("fields", P), ("field_ld", I32), ("perm_slots", I32),
+                ("perm", P), ("packed_j", P), ("packed_j_elems", I64),
+                ("items", P), ("num_items", I32),
+                ("variant_start", I32 * 8), ("variant_count", I32 * 8)]
+
+
+class HostTables(ctypes.Structure):
+    _fields_ = [("n", P), ("replicas", P), ("reads", P), ("chain_off", P),
+                ("j_off", P), ("ld", P)]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("seed", U64), ("update", I32), ("use_pt", I32),
+                ("log_omega_stride", I32), ("best_global", I32),
+                ("phases", I32), ("pad_", I32)]
+
+
+class AisOptions(ctypes.Structure):
+    _fields_ = [("seed", U64), ("update", I32), ("reference", I32),
+                ("order", I32), ("num_temps", I32), ("p", ctypes.c_double)]
+
+
+_lib = None
+
+
+class LibraryError(RuntimeError):
+    pass
+
+
+def load() -> ctypes.CDLL:
+    """Load the CUDA library; build it first when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+        _build.build()
+    lib = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "pysa_gb_abi_version": ([], ctypes.c_int),
+        "pysa_gb_last_error": ([], ctypes.c_char_p),
+        "pysa_gb_workspace_bytes": ([I32, P, P], ctypes.c_int),
+        "pysa_gb_setup": ([P, P, P, P], ctypes.c_int),
+        "pysa_gb_prepare": ([P, P, P, I32, I32, I32, P], ctypes.c_int),
+        "pysa_gb_sweeps": ([P, P, P, P, I32, P], ctypes.c_int),
+        "pysa_gb_energy64": ([I32, I32, I32, P, P, P, I32, I64, P, P],
+                             ctypes.c_int),
+        "pysa_gb_unpack": ([I32, I32, P, I32, I64, P, I32, P], ctypes.c_int),
+        "pysa_gb_ais": ([P, P, P, P, P, P, P], ctypes.c_int),
+        "pysa_gb_logz_parts": ([I32, I32], I64),
+        "pysa_gb_logz_exact": ([P, ctypes.c_double, P, P, P], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if lib.pysa_gb_abi_version() != 1:
+        raise LibraryError("libpysa_gb ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> int:
+    if rc < 0:
+        msg = load().pysa_gb_last_error().decode(errors="replace")
+        raise LibraryError(f"{what} failed ({rc}): {msg}")
+    return rc
+
+
+def ref(s: ctypes.Structure):
+    return ctypes.byref(s)

@@ -1,0 +1,395 @@
+// abi.cu -- extern "C" entry points of libpysa_gb (declared in
+// include/pysa_gb.h).  Host code only: argument checks, the work list of the
+// sweep kernel, variant dispatch and launches on the caller's stream.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ais_api.h"
+#include "aux.cuh"
+#include "plain_variants.h"
+#include "sweep_plain.cuh"
+
+namespace pysa_gb {
+
+extern const PlainVariant kPlainSmall[4];
+extern const PlainVariant kPlainLarge[4];
+
+const PlainVariant& plain_variant(int v) {
+  return v < 4 ? kPlainSmall[v] : kPlainLarge[v - 4];
+}
+
+int plain_variant_for(int n) {
+  for (int v = 0; v < kNumPlainVariants; ++v)
+    if (n <= 32 * plain_variant(v).nc) return v;
+  return -1;
+}
+
+static int row_floats(int v) {
+  const int nc = plain_variant(v).nc;
+  const int ls = nc < 4 ? 4 : (((nc / 4) & 1) ? nc : nc + 4);
+  return 32 * ls;
+}
+
+static int lane_stride(int v) { return row_floats(v) / 32; }
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* where) {
+  return fail(PYSA_GB_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Per-device, per-variant launch geometry, filled on first use.
+struct VariantInfo {
+  bool ready[2] = {false, false};
+  int blocks_per_sm[2] = {0, 0};
+};
+static VariantInfo g_vinfo[64][kNumPlainVariants];
+
+static int prepare_variant(int v, bool random, int* grid_cap) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev >= 64) return fail(PYSA_GB_ERR_ARG, "device index >= 64");
+  VariantInfo& vi = g_vinfo[dev][v];
+  const PlainVariant& pv = plain_variant(v);
+  if (!vi.ready[random]) {
+    const size_t sm = pv.smem(random);
+    e = cudaFuncSetAttribute(pv.func(random),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+    int bps = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pv.func(random),
+                                                      pv.w * 32, sm);
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+    if (bps < 1) return fail(PYSA_GB_ERR_SIZE, "sweep kernel does not fit");
+    vi.blocks_per_sm[random] = bps;
+    vi.ready[random] = true;
+  }
+  int sms = 0;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "SM count");
+  *grid_cap = sms * vi.blocks_per_sm[random];
+  return PYSA_GB_OK;
+}
+
+}  // namespace pysa_gb
+
+using namespace pysa_gb;
+
+extern "C" {
+
+int pysa_gb_abi_version(void) { return PYSA_GB_ABI_VERSION; }
+
+const char* pysa_gb_last_error(void) { return g_last_error.c_str(); }
+
+int pysa_gb_workspace_bytes(int32_t num_instances,
+                            const pysa_gb_host_tables* host, int64_t out[3]) {
+  if (num_instances < 0 || !out ||
+      (num_instances > 0 &&
+       (!host || !host->n || !host->replicas || !host->reads)))
+    return fail(PYSA_GB_ERR_ARG, "workspace_bytes: null argument");
+  const int32_t* n_host = host ? host->n : nullptr;
+  const int32_t* replicas_host = host ? host->replicas : nullptr;
+  const int32_t* reads_host = host ? host->reads : nullptr;
+  int64_t packed = 0, items = 0;
+  int max_nc = 1;
+  for (int i = 0; i < num_instances; ++i) {
+    const int n = n_host[i];
+    if (n < 1) return fail(PYSA_GB_ERR_ARG, "instance with n < 1");
+    if (n > PYSA_GB_MAX_N)
+      return fail(PYSA_GB_ERR_SIZE, "n exceeds PYSA_GB_MAX_N");
+    if (replicas_host[i] < 1 || replicas_host[i] > kMaxReplicas)
+      return fail(PYSA_GB_ERR_SIZE, "replicas must be in [1, 512]");
+    if (reads_host[i] < 0) return fail(PYSA_GB_ERR_ARG, "negative reads");
+    const int v = plain_variant_for(n);
+    const PlainVariant& pv = plain_variant(v);
+    packed += (int64_t)n * row_floats(v);
+    const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
+    const int cpb = pv.gw * pv.w;
+    items += (chains + cpb - 1) / cpb;
+    if (pv.nc > max_nc) max_nc = pv.nc;
+  }
+  out[0] = packed;
+  out[1] = items * (int64_t)(sizeof(SweepItem) / sizeof(int32_t));
+  out[2] = 32 * max_nc;
+  return (int)items;
+}
+
+int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
+                  pysa_gb_workspace* ws, void* stream) {
+  if (!p || !ws || !host || !host->n || !host->replicas || !host->reads ||
+      !host->chain_off || !host->j_off || !host->ld)
+    return fail(PYSA_GB_ERR_ARG, "setup: null argument");
+  const int32_t* n_host = host->n;
+  const int32_t* replicas_host = host->replicas;
+  const int32_t* reads_host = host->reads;
+  const int64_t* chain_off_host = host->chain_off;
+  int64_t need[3];
+  const int items_n = pysa_gb_workspace_bytes(p->num_instances, host, need);
+  if (items_n < 0) return items_n;
+  if (!ws->packed_j || ws->packed_j_elems < need[0])
+    return fail(PYSA_GB_ERR_ARG, "packed_j too small");
+  if (!ws->items || ws->num_items < items_n)
+    return fail(PYSA_GB_ERR_ARG, "items too small");
+  if (ws->field_ld < need[2])
+    return fail(PYSA_GB_ERR_ARG, "field_ld too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  // work list ordered by variant; host-side ranges stored in the workspace
+  std::vector<SweepItem> items;
+  items.reserve(items_n);
+  std::vector<int64_t> poff(p->num_instances);
+  int64_t off = 0;
+  for (int i = 0; i < p->num_instances; ++i) {
+    poff[i] = off;
+    off += (int64_t)n_host[i] * row_floats(plain_variant_for(n_host[i]));
+  }
+  for (int v = 0; v < kNumPlainVariants; ++v) {
+    ws->variant_start[v] = (int32_t)items.size();
+    const PlainVariant& pv = plain_variant(v);
+    const int cpb = pv.gw * pv.w;
+    for (int i = 0; i < p->num_instances; ++i) {
+      if (plain_variant_for(n_host[i]) != v) continue;
+      const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
+      for (int64_t c = 0; c < chains; c += cpb) {
+        SweepItem it;
+        it.inst = i;
+        it.chain0 = (int32_t)(chain_off_host[i] + c);
+        it.nchains = (int32_t)((chains - c) < cpb ? (chains - c) : cpb);
+        it.variant = v;
+        it.poff_lo = (int32_t)(uint32_t)(poff[i] & 0xffffffffll);
+        it.poff_hi = (int32_t)(poff[i] >> 32);
+        it.pad0 = it.pad1 = 0;
+        items.push_back(it);
+      }
+    }
+    ws->variant_count[v] = (int32_t)items.size() - ws->variant_start[v];
+  }
+  if (!items.empty()) {
+    cudaError_t e = cudaMemcpyAsync(ws->items, items.data(),
+                                    items.size() * sizeof(SweepItem),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy work list");
+  }
+  // couplings into the packed row layout, per instance
+  for (int i = 0; i < p->num_instances; ++i) {
+    const int v = plain_variant_for(n_host[i]);
+    if (host->ld[i] < n_host[i])
+      return fail(PYSA_GB_ERR_ARG, "ld < n");
+    launch_pack_rows(p->J + host->j_off[i], host->ld[i], n_host[i],
+                     plain_variant(v).nc, lane_stride(v),
+                     ws->packed_j + poff[i], st);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "pack couplings");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_prepare(const pysa_gb_problems* p, pysa_gb_state* s,
+                    pysa_gb_workspace* ws, int32_t set_energies,
+                    int32_t init_best, int32_t best_global, void* stream) {
+  if (!p || !s || !ws || !ws->fields)
+    return fail(PYSA_GB_ERR_ARG, "prepare: null argument");
+  PrepArgs a;
+  a.p = *p;
+  a.s = *s;
+  a.fields = ws->fields;
+  a.field_ld = ws->field_ld;
+  a.set_energies = set_energies;
+  a.init_best = init_best;
+  a.best_global = best_global;
+  launch_prepare(a, (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "prepare");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
+                   pysa_gb_workspace* ws, const pysa_gb_options* o,
+                   int32_t num_sweeps, void* stream) {
+  if (!p || !s || !ws || !o)
+    return fail(PYSA_GB_ERR_ARG, "sweeps: null argument");
+  if (num_sweeps < 0) return fail(PYSA_GB_ERR_ARG, "negative sweep count");
+  const bool random = o->update == PYSA_GB_RANDOM;
+  if (random && (!ws->perm || ws->perm_slots < 1))
+    return fail(PYSA_GB_ERR_ARG, "random order needs a perm workspace");
+  if (o->log_omega_stride > 0 && !s->log_omega)
+    return fail(PYSA_GB_ERR_ARG, "log_omega buffer missing");
+  cudaStream_t st = (cudaStream_t)stream;
+  int caps[kNumPlainVariants];
+  for (int v = 0; v < kNumPlainVariants; ++v) {
+    caps[v] = 0;
+    if (ws->variant_count[v] > 0) {
+      const int rc = prepare_variant(v, random, &caps[v]);
+      if (rc != PYSA_GB_OK) return rc;
+    }
+  }
+  PlainArgs a;
+  a.p = *p;
+  a.s = *s;
+  a.packed_j = ws->packed_j;
+  a.perm = ws->perm;
+  a.fields = ws->fields;
+  a.field_ld = ws->field_ld;
+  a.perm_slots = ws->perm_slots > 0 ? ws->perm_slots : 1;
+  a.update = o->update;
+  a.seed = o->seed;
+  XArgs x;
+  x.p = *p;
+  x.s = *s;
+  x.seed = o->seed;
+  x.use_pt = o->use_pt;
+  x.log_omega_stride = o->log_omega_stride;
+  PermArgs pa;
+  pa.p = *p;
+  pa.sweep_counter = s->sweep_counter;
+  pa.perm = ws->perm;
+  pa.perm_slots = a.perm_slots;
+  pa.seed = o->seed;
+  const int phases = o->phases ? o->phases : 3;
+  for (int sw = 0; sw < num_sweeps; ++sw) {
+    for (int v = 0; (phases & 1) && v < kNumPlainVariants; ++v) {
+      if (v == 0 && random) launch_perm(pa, st);
+      const int count = ws->variant_count[v];
+      if (count == 0) continue;
+      a.items = reinterpret_cast<const SweepItem*>(ws->items) +
+                ws->variant_start[v];
+      a.num_items = count;
+      const int grid = count < caps[v] ? count : caps[v];
+      cudaError_t e = plain_variant(v).launch(a, random, grid, st);
+      if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+    }
+    if (phases & 2) launch_exchange(x, st);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "exchange launch");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_energy64(int32_t problem_type, int32_t n, int32_t ld64,
+                     const double* J64, const double* h64,
+                     const uint32_t* spins, int32_t words, int64_t count,
+                     double* out, void* stream) {
+  if (!J64 || !h64 || !spins || !out || n < 1 || ld64 < n || count < 0 ||
+      words < (n + 31) / 32)
+    return fail(PYSA_GB_ERR_ARG, "energy64: bad argument");
+  launch_energy64(problem_type, n, ld64, J64, h64, spins, words, count, out,
+                  (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "energy64");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_unpack(int32_t problem_type, int32_t n, const uint32_t* spins,
+                   int32_t words, int64_t count, float* out, int32_t out_ld,
+                   void* stream) {
+  if (!spins || !out || n < 1 || out_ld < n || count < 0 ||
+      words < (n + 31) / 32)
+    return fail(PYSA_GB_ERR_ARG, "unpack: bad argument");
+  launch_unpack(problem_type, n, spins, words, count, out, out_ld,
+                (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "unpack");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_ais(const pysa_gb_problems* p, pysa_gb_state* s,
+                pysa_gb_workspace* ws, const pysa_gb_ais_options* o,
+                const float* temps, double* log_w, void* stream) {
+  if (!p || !s || !ws || !o || !temps || !log_w || !ws->fields)
+    return fail(PYSA_GB_ERR_ARG, "ais: null argument");
+  if (p->num_instances != 1)
+    return fail(PYSA_GB_ERR_ARG, "ais: exactly one instance");
+  if (p->max_n > 1024) return fail(PYSA_GB_ERR_SIZE, "ais: n > 1024");
+  if (o->num_temps < 0) return fail(PYSA_GB_ERR_ARG, "ais: num_temps < 0");
+  if (o->update == PYSA_GB_RANDOM &&
+      (!ws->perm || ws->perm_slots < o->num_temps))
+    return fail(PYSA_GB_ERR_ARG, "ais: perm workspace needs num_temps slots");
+  if (o->reference == 1 && !(o->p > 0.0 && o->p < 1.0))
+    return fail(PYSA_GB_ERR_ARG, "ais: bernoulli p must be in (0, 1)");
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t n = 0, ld = 0;
+  int64_t j_off = 0;
+  cudaError_t e = cudaMemcpyAsync(&n, p->n, sizeof(n), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&ld, p->ld, sizeof(ld), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&j_off, p->j_off, sizeof(j_off), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "ais: read instance");
+  if (o->update == PYSA_GB_RANDOM) {
+    e = launch_perm_range(n, p->max_n, 0u, 0u, o->num_temps, o->seed, ws->perm,
+                          st);
+    if (e != cudaSuccess) return cuda_fail(e, "ais: orders");
+  }
+  AisArgs a;
+  a.problem_type = p->problem_type;
+  a.n = n;
+  a.ld = ld;
+  a.words = p->words;
+  a.num_temps = o->num_temps;
+  a.update = o->update;
+  a.ref = o->reference;
+  a.order = o->order;
+  a.inst = 0;
+  a.max_n = p->max_n;
+  a.samples = p->num_chains;
+  a.p = o->p;
+  a.seed = o->seed;
+  a.J = p->J + j_off;
+  a.temps = temps;
+  a.perm = ws->perm;
+  a.fields = ws->fields;
+  a.field_ld = ws->field_ld;
+  a.spins = s->spins;
+  a.energies = s->energies;
+  a.log_w = log_w;
+  if (a.samples > 0) {
+    e = launch_ais(a, st);
+    if (e != cudaSuccess) return cuda_fail(e, "ais launch");
+  }
+  return PYSA_GB_OK;
+}
+
+static const int kLogzChunkBits = 12;
+
+int64_t pysa_gb_logz_parts(int32_t num_instances, int32_t max_n) {
+  if (num_instances < 0 || max_n < 1 || max_n > 34) return -1;
+  const int B = max_n < kLogzChunkBits ? max_n : kLogzChunkBits;
+  const int64_t threads = (int64_t)1 << (max_n - B);
+  return (int64_t)num_instances * ((threads + 255) / 256);
+}
+
+int pysa_gb_logz_exact(const pysa_gb_problems* p, double beta,
+                       double* part_max, double* part_sum, void* stream) {
+  if (!p || !part_max || !part_sum)
+    return fail(PYSA_GB_ERR_ARG, "logz: null argument");
+  if (p->max_n < 1 || p->max_n > 34)
+    return fail(PYSA_GB_ERR_SIZE, "logz: n must be in [1, 34]");
+  LogzArgs a;
+  a.problem_type = p->problem_type;
+  a.num_instances = p->num_instances;
+  a.chunk_bits = kLogzChunkBits;
+  a.beta = beta;
+  a.n = p->n;
+  a.ld = p->ld;
+  a.j_off = p->j_off;
+  a.h_off = p->h_off;
+  a.J = p->J;
+  a.h = p->h;
+  a.part_max = part_max;
+  a.part_sum = part_sum;
+  cudaError_t e = launch_logz(a, p->max_n, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "logz launch");
+  return PYSA_GB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,47 @@
+// aux.cuh -- argument blocks and launchers of the kernels around the sweep.
+#pragma once
+#include "common.cuh"
+
+namespace pysa_gb {
+
+// Largest R the exchange kernel stages in shared memory.
+constexpr int kMaxReplicas = 512;
+
+struct PrepArgs {
+  pysa_gb_problems p;
+  pysa_gb_state s;
+  float* fields;
+  int32_t field_ld;
+  int32_t set_energies;
+  int32_t init_best;
+  int32_t best_global;
+};
+
+struct XArgs {
+  pysa_gb_problems p;
+  pysa_gb_state s;
+  uint64_t seed;
+  int32_t use_pt;
+  int32_t log_omega_stride;
+};
+
+struct PermArgs {
+  pysa_gb_problems p;
+  const int64_t* sweep_counter;
+  int32_t* perm;
+  int32_t perm_slots;
+  uint64_t seed;
+};
+
+void launch_pack_rows(const float* J, int ld, int n, int nc, int ls,
+                      float* packed, cudaStream_t st);
+void launch_prepare(const PrepArgs& a, cudaStream_t st);
+void launch_exchange(const XArgs& a, cudaStream_t st);
+void launch_perm(const PermArgs& a, cudaStream_t st);
+void launch_energy64(int ptype, int n, int ld, const double* J,
+                     const double* h, const uint32_t* spins, int words,
+                     int64_t count, double* out, cudaStream_t st);
+void launch_unpack(int ptype, int n, const uint32_t* spins, int words,
+                   int64_t count, float* out, int out_ld, cudaStream_t st);
+
+}  // namespace pysa_gb

@@ -1,0 +1,318 @@
+// kernels_aux.cu -- the kernels around the sweep: coupling packing, field and
+// energy preparation, replica exchange + log-omega, visiting orders, f64
+// energies and spin unpacking.
+#include "aux.cuh"
+#include "sweep_plain.cuh"
+
+namespace pysa_gb {
+
+// ------------------------------------------------------------ J packing
+// packed[i][l * LS + m] = J[i][32 m + l] (0 outside the instance).
+__global__ void k_pack_rows(const float* J, int ld, int n, int nc, int ls,
+                            float* packed) {
+  const int row_len = 32 * ls;
+  const int64_t total = (int64_t)n * row_len;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / row_len), r = (int)(e % row_len);
+    const int l = r / ls, m = r % ls;
+    const int col = 32 * m + l;
+    packed[e] = (m < nc && col < n) ? J[(int64_t)i * ld + col] : 0.0f;
+  }
+}
+
+void launch_pack_rows(const float* J, int ld, int n, int nc, int ls,
+                      float* packed, cudaStream_t st) {
+  const int64_t total = (int64_t)n * 32 * ls;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  k_pack_rows<<<blocks, 256, 0, st>>>(J, ld, n, nc, ls, packed);
+}
+
+// -------------------------------------------------- fields and energies
+// Warp per chain.  F_i = sum_j J_ij s_j in f64, from f32 partial sums over 32
+// rows (the products J_ij s_j are exact in f32); H_i = f32(F_i + h_i);
+// E = sum_i s_i (F_i / 2 + h_i)  (pysa/ising.py:37, pysa/qubo.py:37).
+__global__ void k_fields(const PrepArgs a) {
+  const int warps = blockDim.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= a.p.num_chains) return;
+  // instance of chain c: binary search over chain_off
+  int lo = 0, hi = a.p.num_instances - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.p.chain_off[mid] <= c) lo = mid; else hi = mid - 1;
+  }
+  const int inst = lo;
+  const int n = a.p.n[inst], ld = a.p.ld[inst];
+  const bool ising = a.p.problem_type == PYSA_GB_ISING;
+  const float* J = a.p.J + a.p.j_off[inst];
+  const float* h = a.p.h + a.p.h_off[inst];
+  const uint32_t* sw = a.s.spins + c * a.p.words;
+  double e = 0.0;
+  constexpr int TC = 8;  // columns per lane per pass
+  for (int base = 0; base < n; base += 32 * TC) {
+    double F[TC];
+    float part[TC];
+#pragma unroll
+    for (int k = 0; k < TC; ++k) {
+      F[k] = 0.0;
+      part[k] = 0.0f;
+    }
+    for (int j = 0; j < n; ++j) {
+      const uint32_t bit = (sw[j >> 5] >> (j & 31)) & 1u;
+      const float sj = bit ? 1.0f : (ising ? -1.0f : 0.0f);
+      if (sj != 0.0f) {
+        const float* row = J + (int64_t)j * ld;  // J symmetric: J[j][i]
+#pragma unroll
+        for (int k = 0; k < TC; ++k) {
+          const int col = base + 32 * k + lane;
+          if (col < n) part[k] += sj * row[col];
+        }
+      }
+      if ((j & 31) == 31 || j == n - 1) {
+#pragma unroll
+        for (int k = 0; k < TC; ++k) {
+          F[k] += (double)part[k];
+          part[k] = 0.0f;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < TC; ++k) {
+      const int col = base + 32 * k + lane;
+      if (col < n) {
+        const uint32_t bit = (sw[col >> 5] >> (col & 31)) & 1u;
+        const double si = bit ? 1.0 : (ising ? -1.0 : 0.0);
+        e += si * (0.5 * F[k] + (double)h[col]);
+        a.fields[c * a.field_ld + col] = (float)(F[k] + (double)h[col]);
+      }
+    }
+  }
+  e = warp_sum(e);
+  if (lane == 0 && a.set_energies) a.s.energies[c] = (float)e;
+}
+
+// chain_beta from beta_idx (pysa/simulation.py:151-152) and best init.
+__global__ void k_read_init(const PrepArgs a) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= a.p.num_reads) return;
+  const int inst = a.p.read_inst[r];
+  const int R = a.p.replicas[inst];
+  const int64_t base = a.p.chain_off[inst] + (r - a.p.read_off[inst]) * R;
+  const float* betas = a.p.ladder + a.p.ladder_off[inst];
+  for (int k = 0; k < R; ++k)
+    a.s.chain_beta[base + a.s.beta_idx[base + k]] = betas[k];
+  if (a.init_best) {
+    for (int k = 0; k < R; ++k) {
+      const int64_t c = base + k;
+      a.s.best_energy[c] = a.best_global ? __int_as_float(0x7f800000)
+                                         : a.s.energies[c];
+      a.s.best_sweep[c] = 0;
+      for (int w = 0; w < a.p.words; ++w)
+        a.s.best_spins[c * a.p.words + w] = a.s.spins[c * a.p.words + w];
+    }
+  }
+}
+
+void launch_prepare(const PrepArgs& a, cudaStream_t st) {
+  if (a.p.num_chains > 0) {
+    const int warps = 4;
+    const int64_t blocks = (a.p.num_chains + warps - 1) / warps;
+    k_fields<<<(unsigned)blocks, warps * 32, 0, st>>>(a);
+  }
+  if (a.p.num_reads > 0)
+    k_read_init<<<(unsigned)((a.p.num_reads + 127) / 128), 128, 0, st>>>(a);
+}
+
+// ------------------------------------------------------ replica exchange
+// Warp per read.  pysa/utils.py:44-58: pairs (R-1,R-2), (R-2,R-3), ... in
+// order; swap beta_idx when de >= 0 or u < exp(de), de in f32.  Then the
+// per-replica betas of the next sweep and, if requested, get_log_omega
+// (pysa/ais.py:79-112) in f64.  The last block to finish advances the sweep
+// counter.
+constexpr int kXWarps = 4;
+
+// Exchange acceptance u < exp(de) (oracle form), with an f32 log-domain fast
+// path that answers only outside its error band.
+__device__ __forceinline__ bool pt_accept(float de, uint32_t x) {
+  if (de >= 0.0f) return true;
+  if (de < -24.0f) return false;
+  const float uf = __uint2float_rn(x) * 0x1p-32f + 0x1p-33f;
+  const float lf = __logf(uf);
+  const float margin = 3e-5f + 1e-6f * fabsf(de);
+  if (lf < de - margin) return true;
+  if (lf > de + margin) return false;
+  return uniform64(x) < exp((double)de);
+}
+
+__global__ void k_exchange(const XArgs a) {
+  __shared__ float E_s[kXWarps][kMaxReplicas];
+  __shared__ int32_t B_s[kXWarps][kMaxReplicas];
+  __shared__ uint32_t X_s[kXWarps][kMaxReplicas];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r = (int64_t)blockIdx.x * kXWarps + warp;
+  const uint32_t sweep = (uint32_t)(*a.s.sweep_counter);
+  if (r < a.p.num_reads) {
+    const int inst = a.p.read_inst[r];
+    const int R = a.p.replicas[inst];
+    const int64_t lread = r - a.p.read_off[inst];
+    const int64_t base = a.p.chain_off[inst] + lread * R;
+    const float* betas = a.p.ladder + a.p.ladder_off[inst];
+    float* E = E_s[warp];
+    int32_t* B = B_s[warp];
+    uint32_t* X = X_s[warp];
+    for (int k = lane; k < R; k += 32) {
+      E[k] = a.s.energies[base + k];
+      B[k] = a.s.beta_idx[base + k];
+      if (a.use_pt && k < R - 1)
+        X[k] = draw1(a.seed, TAG_PT, (uint32_t)inst, sweep, (uint32_t)lread,
+                     (uint32_t)k);
+    }
+    __syncwarp();
+    if (a.use_pt && R > 1 && lane == 0) {
+      for (int k = 0; k < R - 1; ++k) {
+        const int k1 = R - k - 1, k2 = R - k - 2;
+        const int b1 = B[k1], b2 = B[k2];
+        const float de = __fmul_rn(__fsub_rn(E[b1], E[b2]),
+                                   __fsub_rn(betas[k1], betas[k2]));
+        if (pt_accept(de, X[k])) {
+          B[k1] = b2;
+          B[k2] = b1;
+        }
+      }
+    }
+    __syncwarp();
+    for (int k = lane; k < R; k += 32) {
+      a.s.beta_idx[base + k] = B[k];
+      a.s.chain_beta[base + B[k]] = betas[k];
+    }
+    if (a.log_omega_stride > 0 && lane == 0) {
+      const int32_t* sorted = a.p.ladder_sorted + a.p.ladder_off[inst];
+      double lw = 0.0;
+      float beta_old = 0.0f;
+      for (int q = 1; q < R; ++q) {
+        const float b = betas[sorted[q]];
+        const float e = E[B[sorted[q]]];
+        const float t1 = __fmul_rn(-b, e), t2 = __fmul_rn(-beta_old, e);
+        lw += (double)__fsub_rn(t1, t2);
+        beta_old = b;
+      }
+      a.s.log_omega[r * a.log_omega_stride + sweep] = lw;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const uint32_t t = atomicAdd(a.s.ticket, 1u);
+    if (t == gridDim.x - 1) {
+      *a.s.ticket = 0u;
+      __threadfence();
+      *a.s.sweep_counter += 1;
+    }
+  }
+}
+
+void launch_exchange(const XArgs& a, cudaStream_t st) {
+  const int64_t blocks = (a.p.num_reads + kXWarps - 1) / kXWarps;
+  k_exchange<<<(unsigned)(blocks > 0 ? blocks : 1), kXWarps * 32, 0, st>>>(a);
+}
+
+// ---------------------------------------------------- visiting orders
+// Fisher-Yates for (instance, sweep): j = floor(x (i+1) / 2^32); draws made
+// in parallel, swaps by one thread.  Block per instance.
+__global__ void k_perm(const PermArgs a) {
+  extern __shared__ int32_t sh[];
+  const int inst = blockIdx.x;
+  const int n = a.p.n[inst];
+  const uint32_t sweep = (uint32_t)(*a.sweep_counter);
+  int32_t* p = sh;
+  uint32_t* x = reinterpret_cast<uint32_t*>(sh + a.p.max_n);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    p[i] = i;
+    x[i] = draw1(a.seed, TAG_PERM, (uint32_t)inst, sweep, 0u, (uint32_t)i);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = n - 1; i > 0; --i) {
+      const int j = (int)(((uint64_t)x[i] * (uint64_t)(i + 1)) >> 32);
+      const int32_t t = p[i];
+      p[i] = p[j];
+      p[j] = t;
+    }
+  }
+  __syncthreads();
+  int32_t* out = a.perm + ((int64_t)(sweep % (uint32_t)a.perm_slots) *
+                               a.p.num_instances + inst) * (int64_t)a.p.max_n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = p[i];
+}
+
+void launch_perm(const PermArgs& a, cudaStream_t st) {
+  const size_t sm = sizeof(int32_t) * 2 * (size_t)a.p.max_n;
+  k_perm<<<a.p.num_instances, 256, sm, st>>>(a);
+}
+
+// ----------------------------------------------------------- f64 energy
+// Warp per state: E = sum_i s_i (sum_j J_ij s_j / 2 + h_i) in f64.
+__global__ void k_energy64(int ptype, int n, int ld, const double* J,
+                           const double* h, const uint32_t* spins, int words,
+                           int64_t count, double* out) {
+  const int warps = blockDim.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= count) return;
+  const uint32_t* sw = spins + c * words;
+  const bool ising = ptype == PYSA_GB_ISING;
+  double e = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double si = ((sw[i >> 5] >> (i & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+    if (si == 0.0) continue;
+    double f = 0.0;
+    const double* row = J + (int64_t)i * ld;
+    for (int j = 0; j < n; ++j) {
+      const double sj =
+          ((sw[j >> 5] >> (j & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+      f += row[j] * sj;
+    }
+    e += si * (0.5 * f + h[i]);
+  }
+  e = warp_sum(e);
+  if (lane == 0) out[c] = e;
+}
+
+void launch_energy64(int ptype, int n, int ld, const double* J,
+                     const double* h, const uint32_t* spins, int words,
+                     int64_t count, double* out, cudaStream_t st) {
+  const int warps = 4;
+  const int64_t blocks = (count + warps - 1) / warps;
+  if (blocks > 0)
+    k_energy64<<<(unsigned)blocks, warps * 32, 0, st>>>(ptype, n, ld, J, h,
+                                                        spins, words, count,
+                                                        out);
+}
+
+// ---------------------------------------------------------------- unpack
+__global__ void k_unpack(int ptype, int n, const uint32_t* spins, int words,
+                         int64_t count, float* out, int out_ld) {
+  const int64_t total = count * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / n;
+    const int j = (int)(e % n);
+    const uint32_t bit = (spins[c * words + (j >> 5)] >> (j & 31)) & 1u;
+    out[c * out_ld + j] = bit ? 1.0f : (ptype == PYSA_GB_ISING ? -1.0f : 0.0f);
+  }
+}
+
+void launch_unpack(int ptype, int n, const uint32_t* spins, int words,
+                   int64_t count, float* out, int out_ld, cudaStream_t st) {
+  const int64_t total = count * n;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  if (blocks > 0)
+    k_unpack<<<(unsigned)blocks, 256, 0, st>>>(ptype, n, spins, words, count,
+                                               out, out_ld);
+}
+
+}  // namespace pysa_gb

@@ -1,0 +1,264 @@
+"""Device-resident parallel-tempering batch over the C ABI.
+
+`PTBatch` owns the device buffers of a batch of dense instances (uneven sizes
+allowed), their chains (instance x read x replica) and the workspace, and
+drives libpysa_gb: set-up (coupling packing, work list), preparation (local
+fields and energies in f64), sweeps with replica exchange (optionally replayed
+from a captured CUDA graph) and read-back.  PyTorch only provides device
+memory and the stream.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, ref
+
+
+def pack_spins(states: np.ndarray, problem_type: str, words: int) -> np.ndarray:
+    """[..., n] float (+-1 or 0/1) -> [..., words] uint32 bit-packed."""
+    st = np.asarray(states)
+    bits = (st > 0) if problem_type == "ising" else (st != 0)
+    flat = bits.reshape(-1, st.shape[-1])
+    by = np.packbits(flat, axis=1, bitorder="little")
+    out = np.zeros((flat.shape[0], words * 4), np.uint8)
+    out[:, :by.shape[1]] = by
+    return out.view("<u4").reshape(st.shape[:-1] + (words,))
+
+
+def unpack_spins(words_arr: np.ndarray, n: int, problem_type: str,
+                 dtype) -> np.ndarray:
+    """[..., words] uint32 -> [..., n] values +-1 (Ising) or 0/1 (QUBO)."""
+    w = np.ascontiguousarray(words_arr, dtype="<u4")
+    by = w.view(np.uint8).reshape(w.shape[:-1] + (w.shape[-1] * 4,))
+    bits = np.unpackbits(by, axis=-1, bitorder="little")[..., :n]
+    if problem_type == "ising":
+        return (2 * bits.astype(np.int8) - 1).astype(dtype)
+    return bits.astype(dtype)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr() if t is not None and t.numel() > 0 else 0
+
+
+@dataclass
+class Instance:
+    J: np.ndarray       # [n, n] couplings, zero diagonal
+    h: np.ndarray       # [n]
+    ladder: np.ndarray  # [R] betas in slot order
+    reads: int
+
+
+class PTBatch:
+
+    def __init__(self, problem_type: str, instances: list[Instance],
+                 device: torch.device | str | None = None,
+                 perm_slots: int = 1):
+        if not torch.cuda.is_available():
+            raise RuntimeError(
+                "pysa_gb300 needs a CUDA GPU: the sweeps run only as "
+                "sm_103a kernels (no CPU path)")
+        self.lib = _lib.load()
+        self.device = torch.device(device or "cuda")
+        self.problem_type = problem_type
+        self.ptype = _lib.ISING if problem_type == "ising" else _lib.QUBO
+        I = len(instances)
+        self.instances = instances
+        n = np.array([len(x.h) for x in instances], np.int32)
+        R = np.array([len(x.ladder) for x in instances], np.int32)
+        Rd = np.array([x.reads for x in instances], np.int32)
+        ld = ((n + 3) // 4 * 4).astype(np.int32)
+        j_off = np.zeros(I, np.int64)
+        h_off = np.zeros(I, np.int64)
+        chain_off = np.zeros(I, np.int64)
+        read_off = np.zeros(I, np.int64)
+        ladder_off = np.zeros(I, np.int64)
+        jt, ht, lt, ls = 0, 0, 0, 0
+        ct, rt = 0, 0
+        for i in range(I):
+            j_off[i], h_off[i], ladder_off[i] = jt, ht, lt
+            chain_off[i], read_off[i] = ct, rt
+            jt += int(n[i]) * int(ld[i])
+            ht += int(n[i])
+            lt += int(R[i])
+            ct += int(R[i]) * int(Rd[i])
+            rt += int(Rd[i])
+        self.n, self.R, self.Rd, self.ld = n, R, Rd, ld
+        self.chain_off, self.read_off = chain_off, read_off
+        self.num_chains, self.num_reads = ct, rt
+        self.max_n = int(n.max()) if I else 1
+        self.words = (self.max_n + 31) // 32
+        Jcat = np.zeros(max(jt, 1), np.float32)
+        hcat = np.zeros(max(ht, 1), np.float32)
+        lad = np.zeros(max(lt, 1), np.float32)
+        lsort = np.zeros(max(lt, 1), np.int32)
+        for i, x in enumerate(instances):
+            ni, li = int(n[i]), int(ld[i])
+            blk = np.zeros((ni, li), np.float32)
+            # transposed: row j = change of every field when spin j flips
+            blk[:, :ni] = np.asarray(x.J, np.float32).T
+            Jcat[j_off[i]:j_off[i] + ni * li] = blk.ravel()
+            hcat[h_off[i]:h_off[i] + ni] = np.asarray(x.h, np.float32)
+            lad[ladder_off[i]:ladder_off[i] + R[i]] = x.ladder
+            lsort[ladder_off[i]:ladder_off[i] + R[i]] = np.argsort(
+                np.asarray(x.ladder, np.float32), kind="stable")
+        read_inst = np.repeat(np.arange(I, dtype=np.int32), Rd)
+        dev = self.device
+
+        def T(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+        self._t = dict(n=T(n), R=T(R), Rd=T(Rd), ld=T(ld), j_off=T(j_off),
+                       h_off=T(h_off), chain_off=T(chain_off),
+                       read_off=T(read_off), ladder_off=T(ladder_off),
+                       read_inst=T(read_inst if rt else np.zeros(1, np.int32)),
+                       J=T(Jcat), h=T(hcat), ladder=T(lad), lsort=T(lsort))
+        t = self._t
+        self.p = _lib.Problems(
+            self.ptype, I, self.max_n, self.words, ct, rt, _ptr(t["n"]),
+            _ptr(t["R"]), _ptr(t["Rd"]), _ptr(t["j_off"]), _ptr(t["ld"]),
+            _ptr(t["h_off"]), _ptr(t["chain_off"]), _ptr(t["read_off"]),
+            _ptr(t["ladder_off"]), _ptr(t["read_inst"]), _ptr(t["J"]),
+            _ptr(t["h"]), _ptr(t["ladder"]), _ptr(t["lsort"]))
+        C, W = max(ct, 1), self.words
+        z = lambda *s, dt: torch.zeros(*s, dtype=dt, device=dev)  # noqa: E731
+        self.spins = z(C, W, dt=torch.int32)
+        self.energies = z(C, dt=torch.float32)
+        self.beta_idx = z(C, dt=torch.int32)
+        self.chain_beta = z(C, dt=torch.float32)
+        self.best_energy = z(C, dt=torch.float32)
+        self.best_sweep = z(C, dt=torch.int32)
+        self.best_spins = z(C, W, dt=torch.int32)
+        self.sweep_counter = z(1, dt=torch.int64)
+        self.status = z(1, dt=torch.int32)
+        self.ticket = z(1, dt=torch.int32)
+        self.log_omega = None
+        self.s = _lib.State(_ptr(self.spins), _ptr(self.energies),
+                            _ptr(self.beta_idx), _ptr(self.chain_beta),
+                            _ptr(self.best_energy), _ptr(self.best_sweep),
+                            _ptr(self.best_spins), 0, _ptr(self.sweep_counter),
+                            _ptr(self.status), _ptr(self.ticket))
+        # workspace
+        self._host = (n, R, Rd, chain_off, j_off, ld)
+        ht_ = _lib.HostTables(*(a.ctypes.data for a in self._host))
+        need = (ctypes.c_int64 * 3)()
+        items = check(self.lib.pysa_gb_workspace_bytes(I, ref(ht_), need),
+                      "workspace sizing")
+        self.field_ld = int(need[2])
+        self.fields = z(C, self.field_ld, dt=torch.float32)
+        self.packed_j = z(max(int(need[0]), 1), dt=torch.float32)
+        self.items = z(max(int(need[1]), 8), dt=torch.int32)
+        self.perm_slots = max(int(perm_slots), 1)
+        self.perm = z(self.perm_slots * I * self.max_n, dt=torch.int32)
+        self.ws = _lib.Workspace(_ptr(self.fields), self.field_ld,
+                                 self.perm_slots, _ptr(self.perm),
+                                 _ptr(self.packed_j), int(need[0]),
+                                 _ptr(self.items), max(items, 1))
+        self._stream = torch.cuda.current_stream(dev)
+        check(self.lib.pysa_gb_setup(ref(self.p), ref(ht_), ref(self.ws),
+                                     self._stream.cuda_stream), "setup")
+        self._graphs = {}
+
+    # ------------------------------------------------------------ states
+    def set_states(self, spins_words: np.ndarray, energies=None,
+                   best_global: bool = False):
+        """Load chains ([C, words] uint32) and optional energies [C]; then
+        compute local fields (and energies when not given) on the GPU."""
+        st = self._stream.cuda_stream
+        w = np.ascontiguousarray(spins_words, "<u4").reshape(self.num_chains,
+                                                            self.words)
+        self.spins.copy_(torch.from_numpy(w.view(np.int32)))
+        if energies is not None:
+            self.energies.copy_(torch.from_numpy(
+                np.ascontiguousarray(energies, np.float32).reshape(-1)))
+        bidx = np.concatenate([
+            np.tile(np.arange(self.R[i], dtype=np.int32), self.Rd[i])
+            for i in range(len(self.instances))
+        ]) if self.num_chains else np.zeros(1, np.int32)
+        self.beta_idx.copy_(torch.from_numpy(bidx))
+        self.sweep_counter.zero_()
+        self.status.zero_()
+        self.ticket.zero_()
+        self.best_global = bool(best_global)
+        check(self.lib.pysa_gb_prepare(ref(self.p), ref(self.s), ref(self.ws),
+                                       int(energies is None), 1,
+                                       int(best_global), st), "prepare")
+
+    # ------------------------------------------------------------ sweeps
+    def run(self, num_sweeps: int, *, seed: int, update: str = "sequential",
+            use_pt: bool = True, log_omega: bool = False,
+            graph_chunk: int = 64):
+        upd = _lib.RANDOM if update == "random" else _lib.SEQUENTIAL
+        stride = int(num_sweeps) if log_omega else 0
+        if log_omega:
+            self.log_omega = torch.zeros(max(self.num_reads, 1), max(stride, 1),
+                                         dtype=torch.float64,
+                                         device=self.device)
+            self.s.log_omega = _ptr(self.log_omega)
+        else:
+            self.s.log_omega = 0
+        opts = _lib.Options(seed & ((1 << 64) - 1), upd, int(use_pt), stride,
+                            int(self.best_global), 0, 0)
+        st = self._stream.cuda_stream
+        # first call with zero sweeps sets kernel attributes outside capture
+        check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s), ref(self.ws),
+                                      ref(opts), 0, st), "sweeps")
+        remaining = int(num_sweeps)
+        chunk = int(graph_chunk)
+        if chunk > 1 and remaining >= 2 * chunk:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                cs = torch.cuda.current_stream(self.device).cuda_stream
+                check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s),
+                                              ref(self.ws), ref(opts), chunk,
+                                              cs), "sweeps (capture)")
+            for _ in range(remaining // chunk):
+                g.replay()
+            remaining %= chunk
+            self._graphs["last"] = g  # keep alive until the stream drains
+        if remaining:
+            check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s),
+                                          ref(self.ws), ref(opts), remaining,
+                                          st), "sweeps")
+
+    def check_status(self):
+        code = int(self.status.item())
+        if code != 0:
+            raise _lib.LibraryError(
+                f"device reported status {code} (a bounded wait ran out)")
+
+    # --------------------------------------------------------- read back
+    def fetch(self) -> dict:
+        torch.cuda.synchronize(self.device)
+        self.check_status()
+        out = dict(
+            spins=self.spins.cpu().numpy().view("<u4"),
+            energies=self.energies.cpu().numpy(),
+            beta_idx=self.beta_idx.cpu().numpy(),
+            best_energy=self.best_energy.cpu().numpy(),
+            best_sweep=self.best_sweep.cpu().numpy(),
+            best_spins=self.best_spins.cpu().numpy().view("<u4"),
+        )
+        if self.log_omega is not None:
+            out["log_omega"] = self.log_omega.cpu().numpy()
+        return out
+
+    def energy64(self, inst: int, J64: np.ndarray, h64: np.ndarray,
+                 spins_words: torch.Tensor) -> np.ndarray:
+        """f64 energies of device bit-packed states with f64 couplings."""
+        n = int(self.n[inst])
+        Jd = torch.from_numpy(np.ascontiguousarray(J64, np.float64)).to(
+            self.device)
+        hd = torch.from_numpy(np.ascontiguousarray(h64, np.float64)).to(
+            self.device)
+        cnt = spins_words.shape[0]
+        out = torch.empty(cnt, dtype=torch.float64, device=self.device)
+        check(self.lib.pysa_gb_energy64(self.ptype, n, n, _ptr(Jd), _ptr(hd),
+                                        _ptr(spins_words), self.words, cnt,
+                                        _ptr(out), self._stream.cuda_stream),
+              "energy64")
+        return out.cpu().numpy()

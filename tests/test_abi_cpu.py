@@ -1,0 +1,131 @@
+"""C-ABI library and host logic, without a GPU (no compute calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "pysa_gb.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pysa_gb_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_header_symbol():
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    names = _header_functions()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), name
+    assert lib.pysa_gb_abi_version() == 1
+
+
+def test_struct_sizes_match_header_layout():
+    from pysa_gb300 import _lib
+    assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 14 * 8
+    assert ctypes.sizeof(_lib.State) == 11 * 8
+    assert ctypes.sizeof(_lib.Options) == 8 + 6 * 4
+    assert ctypes.sizeof(_lib.AisOptions) == 8 + 4 * 4 + 8
+
+
+def _tables(n, R, Rd):
+    from pysa_gb300 import _lib
+    arrs = [np.asarray(n, np.int32), np.asarray(R, np.int32),
+            np.asarray(Rd, np.int32)]
+    return arrs, _lib.HostTables(*(a.ctypes.data for a in arrs), 0, 0, 0)
+
+
+def test_workspace_plan_host_only():
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    arrs, ht = _tables([100, 1024, 3000], [8, 64, 4], [3, 2, 1])
+    out = (ctypes.c_int64 * 3)()
+    items = lib.pysa_gb_workspace_bytes(3, ctypes.byref(ht), out)
+    # 24 chains / 64 per block + 128 / 32 + 4 / 8
+    assert items == 1 + 4 + 1
+    assert out[2] == 4096
+    assert out[1] == items * 8
+
+
+@pytest.mark.parametrize("bad", [([0], [4], [1]), ([5000], [4], [1]),
+                                 ([10], [0], [1]), ([10], [600], [1])])
+def test_workspace_rejects_bad_sizes(bad):
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    arrs, ht = _tables(*bad)
+    out = (ctypes.c_int64 * 3)()
+    assert lib.pysa_gb_workspace_bytes(1, ctypes.byref(ht), out) < 0
+    assert lib.pysa_gb_last_error()
+
+
+def test_null_arguments_rejected_without_gpu():
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    assert lib.pysa_gb_sweeps(None, None, None, None, 1, None) == -1
+    assert lib.pysa_gb_prepare(None, None, None, 1, 1, 0, None) == -1
+    assert lib.pysa_gb_ais(None, None, None, None, None, None, None) == -1
+    assert lib.pysa_gb_logz_parts(1, 40) == -1
+
+
+def test_pack_unpack_roundtrip():
+    from pysa_gb300.engine import pack_spins, unpack_spins
+    rng = np.random.default_rng(0)
+    for n in (1, 31, 32, 33, 100, 1024, 1025):
+        words = (n + 31) // 32
+        x = (2 * rng.integers(0, 2, (3, 2, n)) - 1).astype(np.float32)
+        w = pack_spins(x, "ising", words)
+        assert w.shape == (3, 2, words)
+        assert (unpack_spins(w, n, "ising", np.float32) == x).all()
+        q = rng.integers(0, 2, (4, n)).astype(np.float64)
+        assert (unpack_spins(pack_spins(q, "qubo", words), n, "qubo",
+                             np.float64) == q).all()
+        # bit j of word j // 32 holds spin j
+        j = n - 1
+        e = np.zeros((1, n))
+        e[0, j] = 1
+        assert pack_spins(e, "qubo", words)[0, j // 32] == 1 << (j % 32)
+
+
+def test_solver_argument_errors_match_reference():
+    from pysa_gb300 import Solver
+    P = np.zeros((4, 4))
+    with pytest.raises(ValueError):
+        Solver(P, "spin")
+    with pytest.raises(ValueError):
+        Solver(np.zeros((4, 3)), "ising")
+    with pytest.raises(ValueError):
+        Solver(np.triu(np.ones((4, 4)), 1), "ising")
+    s = Solver(P, "ising")
+    with pytest.raises(ValueError):
+        s.metropolis_update(num_sweeps=2, num_replicas=3, temps=[1, 2])
+    with pytest.raises(ValueError):
+        s.metropolis_update(num_sweeps=2, initialize_strategy="zeros")
+    with pytest.raises(ValueError):
+        s.metropolis_update(num_sweeps=2, update_strategy="spiral")
+    with pytest.raises(ValueError):
+        s.metropolis_update(num_sweeps=2, temps=[1.0, 2.0], beta0=True)
+    with pytest.raises(ValueError):
+        s.metropolis_update(num_sweeps=2, num_replicas=2,
+                            initialize_strategy=np.ones((3, 4)))
+    with pytest.raises(ValueError):
+        s.annealed_importance(4, 4, "gaussian")
+
+
+def test_ais_host_helpers_match_reference_formulas():
+    from pysa_gb300 import ais
+    lw = np.array([0.3, -1.2, 2.5])
+    want = lw.max() - np.log(3) + 5.0 + np.log(np.exp(lw - lw.max()).sum())
+    assert abs(ais.omegas_to_partition(lw, 5.0) - want) < 1e-12
+    st = np.array([1, -1, -1, 1])
+    p = 0.3
+    # flipping bit 1 (-1 -> +1) raises the count of ones from 2 to 3
+    assert abs(ais.bernoulli_ref_prob(st, p, 1) - p**1 * (1 - p)**3) < 1e-15
+    assert abs(ais.bernoulli_ref_prob(st, p) - p**2 * (1 - p)**2) < 1e-15
+    g = golden("pt_ising_logz")
+    lo = ais.get_log_omega(g["betas"], g["beta_idx"][0], g["energies"][0])
+    assert np.isfinite(lo)
