@@ -118,6 +118,18 @@ typedef struct {
   int32_t num_items;      /* capacity of items, in work items */
   int32_t variant_start[8]; /* host: first work item of each kernel variant */
   int32_t variant_count[8]; /* host: work items of each kernel variant */
+  /* tensor-core blocked sweep (pysa_gb_tc_setup); tc_enabled = 0 disables */
+  uint16_t *tc_b;           /* BF16 J tiles (hi[, lo]) in MMA operand order */
+  int64_t tc_b_elems;
+  float *tc_diag;           /* FP32 64x64 diagonal blocks of J */
+  int64_t tc_diag_elems;
+  int32_t *tc_items;        /* [tc_num_items, 8] work list (128/F chains) */
+  int32_t tc_num_items;
+  int32_t tc_terms;         /* 1: J exact in BF16, 2: J = J_hi + J_lo */
+  int32_t tc_enabled;       /* 1: sequential sweeps use the tensor cores */
+  int32_t tc_variant_start[3]; /* host: items of fold F = 1, 2, 4 */
+  int32_t tc_variant_count[3];
+  int32_t pad_;
 } pysa_gb_workspace;
 
 /* Host copies of the per-instance tables, used to plan the work list. */
@@ -157,6 +169,17 @@ int pysa_gb_workspace_bytes(int32_t num_instances,
                             const pysa_gb_host_tables *host, int64_t out[3]);
 int pysa_gb_setup(const pysa_gb_problems *p, const pysa_gb_host_tables *host,
                   pysa_gb_workspace *ws, void *stream);
+
+/* Tensor-core blocked sweep (sequential order, 64 <= n <= 2048): sizes of
+ * tc_b, tc_diag and tc_items (int32 entries) for `terms` BF16 terms, and the
+ * set-up that packs them.  Returns the number of tc work items, or
+ * PYSA_GB_ERR_SIZE when an instance is outside the supported range. */
+int pysa_gb_tc_workspace(int32_t num_instances,
+                         const pysa_gb_host_tables *host, int32_t terms,
+                         int64_t out[3]);
+int pysa_gb_tc_setup(const pysa_gb_problems *p,
+                     const pysa_gb_host_tables *host, pysa_gb_workspace *ws,
+                     void *stream);
 
 /* Local fields H = J s + h for every chain, accumulated in f64 from f32
  * products, and (if set_energies) energies E = s.(J s / 2 + h)

@@ -39,7 +39,12 @@ class Workspace(ctypes.Structure):
     _fields_ = [("fields", P), ("field_ld", I32), ("perm_slots", I32),
                 ("perm", P), ("packed_j", P), ("packed_j_elems", I64),
                 ("items", P), ("num_items", I32),
-                ("variant_start", I32 * 8), ("variant_count", I32 * 8)]
+                ("variant_start", I32 * 8), ("variant_count", I32 * 8),
+                ("tc_b", P), ("tc_b_elems", I64), ("tc_diag", P),
+                ("tc_diag_elems", I64), ("tc_items", P),
+                ("tc_num_items", I32), ("tc_terms", I32), ("tc_enabled", I32),
+                ("tc_variant_start", I32 * 3), ("tc_variant_count", I32 * 3),
+                ("pad_", I32)]
 
 
 class HostTables(ctypes.Structure):
@@ -79,6 +84,8 @@ def load() -> ctypes.CDLL:
         "pysa_gb_last_error": ([], ctypes.c_char_p),
         "pysa_gb_workspace_bytes": ([I32, P, P], ctypes.c_int),
         "pysa_gb_setup": ([P, P, P, P], ctypes.c_int),
+        "pysa_gb_tc_workspace": ([I32, P, I32, P], ctypes.c_int),
+        "pysa_gb_tc_setup": ([P, P, P, P], ctypes.c_int),
         "pysa_gb_prepare": ([P, P, P, I32, I32, I32, P], ctypes.c_int),
         "pysa_gb_sweeps": ([P, P, P, P, I32, P], ctypes.c_int),
         "pysa_gb_energy64": ([I32, I32, I32, P, P, P, I32, I64, P, P],

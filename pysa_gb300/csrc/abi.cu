@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "ais_api.h"
+#include "tc_api.h"
 #include "aux.cuh"
 #include "plain_variants.h"
 #include "sweep_plain.cuh"
@@ -193,6 +194,88 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   return PYSA_GB_OK;
 }
 
+int pysa_gb_tc_workspace(int32_t num_instances,
+                         const pysa_gb_host_tables* host, int32_t terms,
+                         int64_t out[3]) {
+  if (num_instances < 0 || !out || (terms != 1 && terms != 2) ||
+      (num_instances > 0 && (!host || !host->n || !host->replicas ||
+                             !host->reads)))
+    return fail(PYSA_GB_ERR_ARG, "tc_workspace: bad argument");
+  int64_t b = 0, d = 0, items = 0;
+  for (int i = 0; i < num_instances; ++i) {
+    const int n = host->n[i];
+    if (n < 64 || n > 2048)
+      return fail(PYSA_GB_ERR_SIZE, "tensor-core sweep needs 64 <= n <= 2048");
+    b += tc_b_elems(n, terms);
+    d += tc_diag_elems(n);
+    const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
+    const int cc = tc_chains_per_cta(n);
+    items += (chains + cc - 1) / cc;
+  }
+  out[0] = b;
+  out[1] = d;
+  out[2] = items * (int64_t)(sizeof(TcItem) / sizeof(int32_t));
+  return (int)items;
+}
+
+int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
+                     pysa_gb_workspace* ws, void* stream) {
+  if (!p || !host || !ws || !host->chain_off || !host->j_off || !host->ld)
+    return fail(PYSA_GB_ERR_ARG, "tc_setup: null argument");
+  int64_t need[3];
+  const int items_n =
+      pysa_gb_tc_workspace(p->num_instances, host, ws->tc_terms, need);
+  if (items_n < 0) return items_n;
+  if (!ws->tc_b || ws->tc_b_elems < need[0] || !ws->tc_diag ||
+      ws->tc_diag_elems < need[1] || !ws->tc_items ||
+      ws->tc_num_items < items_n)
+    return fail(PYSA_GB_ERR_ARG, "tc workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<int64_t> boff(p->num_instances), doff(p->num_instances);
+  int64_t bo = 0, dd = 0;
+  for (int i = 0; i < p->num_instances; ++i) {
+    boff[i] = bo;
+    doff[i] = dd;
+    bo += tc_b_elems(host->n[i], ws->tc_terms);
+    dd += tc_diag_elems(host->n[i]);
+  }
+  std::vector<TcItem> items;
+  const int folds[3] = {1, 2, 4};
+  for (int v = 0; v < 3; ++v) {
+    ws->tc_variant_start[v] = (int32_t)items.size();
+    for (int i = 0; i < p->num_instances; ++i) {
+      if (tc_fold_for(host->n[i]) != folds[v]) continue;
+      const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
+      const int cc = tc_chains_per_cta(host->n[i]);
+      for (int64_t c = 0; c < chains; c += cc) {
+        TcItem it;
+        it.inst = i;
+        it.chain0 = (int32_t)(host->chain_off[i] + c);
+        it.nchains = (int32_t)((chains - c) < cc ? (chains - c) : cc);
+        it.fold = folds[v];
+        it.b_off = boff[i];
+        it.diag_off = doff[i];
+        items.push_back(it);
+      }
+    }
+    ws->tc_variant_count[v] = (int32_t)items.size() - ws->tc_variant_start[v];
+  }
+  if (!items.empty()) {
+    cudaError_t e = cudaMemcpyAsync(ws->tc_items, items.data(),
+                                    items.size() * sizeof(TcItem),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy tc work list");
+  }
+  for (int i = 0; i < p->num_instances; ++i) {
+    cudaError_t e = launch_pack_tc(p->J + host->j_off[i], host->ld[i],
+                                   host->n[i], ws->tc_terms, ws->tc_b + boff[i],
+                                   ws->tc_diag + doff[i], st);
+    if (e != cudaSuccess) return cuda_fail(e, "pack tc tiles");
+  }
+  ws->tc_enabled = 1;
+  return PYSA_GB_OK;
+}
+
 int pysa_gb_prepare(const pysa_gb_problems* p, pysa_gb_state* s,
                     pysa_gb_workspace* ws, int32_t set_energies,
                     int32_t init_best, int32_t best_global, void* stream) {
@@ -225,9 +308,10 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
     return fail(PYSA_GB_ERR_ARG, "log_omega buffer missing");
   cudaStream_t st = (cudaStream_t)stream;
   int caps[kNumPlainVariants];
+  const bool tc_path = ws->tc_enabled && !random && ws->tc_items;
   for (int v = 0; v < kNumPlainVariants; ++v) {
     caps[v] = 0;
-    if (ws->variant_count[v] > 0) {
+    if (ws->variant_count[v] > 0 && !tc_path) {
       const int rc = prepare_variant(v, random, &caps[v]);
       if (rc != PYSA_GB_OK) return rc;
     }
@@ -255,8 +339,28 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   pa.perm_slots = a.perm_slots;
   pa.seed = o->seed;
   const int phases = o->phases ? o->phases : 3;
+  const bool use_tc = ws->tc_enabled && !random && ws->tc_items;
+  TcArgs ta;
+  ta.p = *p;
+  ta.s = *s;
+  ta.fields = ws->fields;
+  ta.field_ld = ws->field_ld;
+  ta.terms = ws->tc_terms;
+  ta.tc_b = ws->tc_b;
+  ta.tc_diag = ws->tc_diag;
+  ta.seed = o->seed;
   for (int sw = 0; sw < num_sweeps; ++sw) {
-    for (int v = 0; (phases & 1) && v < kNumPlainVariants; ++v) {
+    if (use_tc && (phases & 1)) {
+      const int folds[3] = {1, 2, 4};
+      for (int v = 0; v < 3; ++v) {
+        if (ws->tc_variant_count[v] == 0) continue;
+        ta.items = reinterpret_cast<const TcItem*>(ws->tc_items) +
+                   ws->tc_variant_start[v];
+        cudaError_t e = launch_tc(ta, folds[v], ws->tc_variant_count[v], st);
+        if (e != cudaSuccess) return cuda_fail(e, "tc sweep launch");
+      }
+    }
+    for (int v = 0; !use_tc && (phases & 1) && v < kNumPlainVariants; ++v) {
       if (v == 0 && random) launch_perm(pa, st);
       const int count = ws->variant_count[v];
       if (count == 0) continue;

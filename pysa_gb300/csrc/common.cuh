@@ -147,6 +147,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
 // Bounded wait: about 2^22 polls (each try_wait already suspends for a
 // hardware time slice), i.e. well over a second, then give up with a status.
 constexpr uint32_t kWaitPolls = 1u << 22;

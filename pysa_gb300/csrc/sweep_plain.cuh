@@ -50,12 +50,6 @@ struct PlainArgs {
   uint64_t seed;
 };
 
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-
 // Wait bounded by wall time (about one second), then report and give up.
 __device__ __forceinline__ bool mbar_wait_timed(uint64_t* bar, uint32_t parity,
                                                 int32_t* status) {

@@ -1,0 +1,491 @@
+// sweep_tc.cu -- blocked delayed-update Metropolis sweep on the tensor cores
+// (tcgen05 + tensor memory, sm_103a).
+//
+// Same sweep as pysa/simulation.py:60-76 with the rule of pysa/ising.py:40-63 /
+// pysa/qubo.py:40-63, sequential order, but the spins are resolved 64 at a
+// time:
+//   * the local fields H of the CTA's chains live in TENSOR MEMORY as an FP32
+//     accumulator: TMEM lane m holds chain c = m % CC, columns of slice
+//     q = m / CC (the n columns are folded into F slices of S <= 512);
+//   * for a block of 64 spins each chain's thread reads its 64 fields
+//     (tcgen05.ld), decides the 64 spins one after another, applying the exact
+//     in-block field corrections from the FP32 64x64 diagonal block of J, and
+//     writes its flips delta in {0, +-1, +-2} (exact in BF16) into the A tile;
+//   * one thread issues the cross-block update H += A * B as tcgen05.mma with
+//     B = J rows of the block split as J_hi + J_lo in BF16 (one term when J is
+//     exactly BF16), FP32 accumulation in TMEM.  The MMA of the tile holding
+//     the next block's columns is committed first so the next decisions start
+//     while the remaining tiles run.
+// B tiles (pre-laid-out in the canonical no-swizzle K-major core-matrix order)
+// and the diagonal blocks stream in through a ring of shared-memory stages by
+// 1-D bulk copies (TMA engine).  Integer couplings make every product and sum
+// exact, so trajectories match the plain sweep bit for bit.
+//
+// Roles: warps 0-3 decide (thread = TMEM lane), warp 4 issues MMAs, warp 5
+// produces stages.  Every wait is bounded; a timeout sets the status word and
+// an abort flag that releases every other wait.
+#include "aux.cuh"
+#include "tc_api.h"
+#include "tc_ptx.cuh"
+
+namespace pysa_gb {
+
+template <int F>
+struct TcCfg {
+  static constexpr int CC = 128 / F;          // chains per CTA
+  static constexpr int NS = F == 4 ? 3 : 4;   // B ring stages
+  static constexpr int WORDS = 16 * F;        // spin words per chain
+  static constexpr size_t A_OFF = 0;
+  static constexpr size_t A_BYTES = (size_t)F * 16384;
+  static constexpr size_t B_OFF = A_OFF + A_BYTES;
+  static constexpr size_t B_STAGE = 32768;
+  static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
+  static constexpr size_t SPIN_OFF = JBB_OFF + 2 * 16384;
+  static constexpr size_t DE_OFF = SPIN_OFF + (size_t)CC * WORDS * 4;
+  static constexpr size_t BETA_OFF = DE_OFF + (size_t)CC * 8;
+  static constexpr size_t BAR_OFF = (BETA_OFF + CC * 4 + 63) / 64 * 64;
+  // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], full[NS], free[NS]
+  static constexpr int NBARS = 7 + 2 * NS;
+  static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
+  static constexpr size_t BYTES = MISC_OFF + 16;
+};
+
+struct TcShared {
+  uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *full, *free_;
+  uint32_t* tmem_slot;
+  volatile int32_t* abort;
+};
+
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
+                                        const TcShared& sh, int32_t* status) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*sh.abort) return false;
+    if (globaltimer_ns() - t0 > 1000000000ull) {
+      set_status(status, PYSA_GB_ERR_TIMEOUT);
+      *sh.abort = 1;
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void named_sync_128() {
+  asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(float d) {
+  // exact for d in {0, +-1, +-2}
+  return __float_as_uint(d) >> 16;
+}
+
+template <int F>
+__global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
+  using C = TcCfg<F>;
+  constexpr int CC = C::CC;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::BAR_OFF);
+  TcShared sh;
+  sh.a_full = bars + 0;
+  sh.mma_done = bars + 1;
+  sh.h_ready = bars + 2;
+  sh.jbb_full = bars + 3;
+  sh.jbb_free = bars + 5;
+  sh.full = bars + 7;
+  sh.free_ = bars + 7 + C::NS;
+  sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
+  sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
+  uint32_t* spins_s = reinterpret_cast<uint32_t*>(smem + C::SPIN_OFF);
+  double* dE_s = reinterpret_cast<double*>(smem + C::DE_OFF);
+  float* beta_s = reinterpret_cast<float*>(smem + C::BETA_OFF);
+  const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
+  const uint32_t smem_base = smem_addr(smem);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t* status = a.s.status;
+  const TcItem item = a.items[blockIdx.x];
+  const int inst = item.inst;
+  const int n = a.p.n[inst];
+  const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
+  const int S = NP / F;
+  const int NB = (n + 63) / 64;
+  const int NT = (S + 255) / 256;
+  const int T = a.terms;
+  const int words = (n + 31) >> 5;
+  const bool ising = a.p.problem_type == PYSA_GB_ISING;
+  const uint32_t sweep = (uint32_t)(*a.s.sweep_counter);
+  const int64_t chain_base = a.p.chain_off[inst];
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)S) ncols <<= 1;
+
+  // ---------------------------------------------------------------- set-up
+  if (warp == 0) {
+    tc::tmem_alloc(sh.tmem_slot, ncols);
+    tc::tmem_relinquish();
+  }
+  if (threadIdx.x == 32) {
+    for (int b = 0; b < C::NBARS; ++b) mbar_init(&bars[b], 1);
+    *sh.abort = 0;
+    fence_mbar_init();
+  }
+  for (int i = threadIdx.x; i < (int)(C::A_BYTES / 16); i += blockDim.x)
+    reinterpret_cast<uint4*>(smem + C::A_OFF)[i] = make_uint4(0, 0, 0, 0);
+  for (int i = threadIdx.x; i < CC * C::WORDS; i += blockDim.x) {
+    const int w = i / CC, c = i % CC;  // layout [word][chain]
+    spins_s[i] = (c < item.nchains && w < words)
+                     ? a.s.spins[(item.chain0 + c) * (int64_t)a.p.words + w]
+                     : 0u;
+  }
+  for (int c = threadIdx.x; c < CC; c += blockDim.x) {
+    dE_s[c] = 0.0;
+    beta_s[c] = c < item.nchains ? a.s.chain_beta[item.chain0 + c] : 0.0f;
+  }
+  fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = *sh.tmem_slot;
+
+  // decision-thread identity: TMEM lane L = slice q, chain c
+  const int L = threadIdx.x;
+  const int q = L / CC, c = L % CC;
+  const bool valid = warp < 4 && c < item.nchains;
+  const int64_t chain = item.chain0 + c;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+
+  if (warp < 4) {  // local fields -> TMEM
+    for (int j0 = 0; j0 < S; j0 += 32) {
+      float v[32];
+      const float* f = a.fields + chain * a.field_ld + q * S + j0;
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        v[i] = (valid && q * S + j0 + i < n) ? f[i] : 0.0f;
+      tc::tmem_st32(taddr + lane_base + j0, v);
+    }
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+
+  const uint32_t idesc_full = tc::idesc_bf16(128, 256);
+
+  if (warp < 4) {
+    // ============================================================ decide
+    const uint32_t chain_local = (uint32_t)(chain - chain_base);
+    const float beta = beta_s[c];
+    // every decision thread runs all NB iterations (named barrier inside);
+    // after an abort the work is skipped
+    for (int t = 0; t < NB; ++t) {
+      const int i0 = 64 * t;
+      const int qt = i0 / S, co = i0 % S;
+      const int kmax = n - i0 < 64 ? n - i0 : 64;
+      bool go = q == qt && !*sh.abort;
+      if (go && t > 0) go = tc_wait(sh.h_ready, (t - 1) & 1, sh, status);
+      if (go) go = tc_wait(&sh.jbb_full[t & 1], (t >> 1) & 1, sh, status);
+      if (go) {
+        tc::fence_after_sync();
+        float h[64];
+        tc::tmem_ld32(taddr + lane_base + co, h);
+        tc::tmem_ld32(taddr + lane_base + co + 32, h + 32);
+        const float4* jb4 = reinterpret_cast<const float4*>(jbb + (t & 1) * 4096);
+        uint32_t w0 = spins_s[(2 * t) * CC + c];
+        uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
+        float dEb = 0.0f;
+        uint32_t pk[32];  // bf16 pairs of the 64 deltas
+        uint32_t x4[4];
+#pragma unroll
+        for (int k = 0; k < 64; ++k) {
+          if ((k & 3) == 0)
+            draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, chain_local,
+                  (uint32_t)((i0 + k) >> 2), x4);
+          const bool s = k < 32 ? ((w0 >> k) & 1u) : ((w1 >> (k - 32)) & 1u);
+          const float hk = h[k];
+          const float dn = ising ? (s ? 2.0f * hk : -2.0f * hk) : (s ? hk : -hk);
+          const bool acc = valid && k < kmax &&
+                           metropolis_accept(dn, beta, x4[k & 3]);
+          const float dl =
+              acc ? (ising ? (s ? -2.0f : 2.0f) : (s ? -1.0f : 1.0f)) : 0.0f;
+          if (acc) {
+            dEb -= dn;
+            if (k < 32) w0 ^= 1u << k; else w1 ^= 1u << (k - 32);
+          }
+          const uint32_t b16 = bf16_bits(dl);
+          if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
+          // exact in-block corrections: h[k2] += dl * J[i0+k][i0+k2], k2 > k
+#pragma unroll
+          for (int g = (k + 1) >> 2; g < 16; ++g) {
+            const float4 jv = jb4[k * 16 + g];
+            if (4 * g + 0 > k) h[4 * g + 0] = fmaf(dl, jv.x, h[4 * g + 0]);
+            if (4 * g + 1 > k) h[4 * g + 1] = fmaf(dl, jv.y, h[4 * g + 1]);
+            if (4 * g + 2 > k) h[4 * g + 2] = fmaf(dl, jv.z, h[4 * g + 2]);
+            if (4 * g + 3 > k) h[4 * g + 3] = fmaf(dl, jv.w, h[4 * g + 3]);
+          }
+        }
+        if (valid) {
+          spins_s[(2 * t) * CC + c] = w0;
+          spins_s[(2 * t + 1) * CC + c] = w1;
+          dE_s[c] += (double)dEb;
+        }
+        // A is single-buffered: the previous block's MMAs must be done
+        const bool a_free =
+            t == 0 || tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
+#pragma unroll
+        for (int qq = 0; qq < F && a_free; ++qq) {
+          const int m = qq * CC + c;  // A row = TMEM lane of (slice qq, chain c)
+          unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                ((m >> 3) * 8) * 128 + (m & 7) * 16;
+#pragma unroll
+          for (int kc = 0; kc < 8; ++kc)
+            *reinterpret_cast<uint4*>(rowp + kc * 128) =
+                make_uint4(pk[4 * kc], pk[4 * kc + 1], pk[4 * kc + 2],
+                           pk[4 * kc + 3]);
+        }
+        fence_proxy_async();
+      }
+      named_sync_128();
+      if (threadIdx.x == 0) {
+        mbar_arrive(sh.a_full);
+        mbar_arrive(&sh.jbb_free[t & 1]);
+      }
+    }
+    // ----------------------------------------------------------- epilogue
+    if (!*sh.abort && NB > 0)
+      tc_wait(sh.mma_done, (NB - 1) & 1, sh, status);
+    tc::fence_after_sync();
+    if (!*sh.abort) {
+      for (int j0 = 0; j0 < S; j0 += 32) {
+        float v[32];
+        tc::tmem_ld32(taddr + lane_base + j0, v);
+        float* f = a.fields + chain * a.field_ld + q * S + j0;
+        if (valid) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            if (q * S + j0 + i < n) f[i] = v[i];
+        }
+      }
+    }
+    tc::fence_before_sync();
+    named_sync_128();
+    if (q == 0 && valid && !*sh.abort) {
+      const float e_new = (float)((double)a.s.energies[chain] + dE_s[c]);
+      a.s.energies[chain] = e_new;
+      const bool improved = e_new < a.s.best_energy[chain];
+      if (improved) {
+        a.s.best_energy[chain] = e_new;
+        a.s.best_sweep[chain] = (int32_t)sweep;
+      }
+      for (int w = 0; w < words; ++w) {
+        const uint32_t v = spins_s[w * CC + c];
+        a.s.spins[chain * a.p.words + w] = v;
+        if (improved) a.s.best_spins[chain * a.p.words + w] = v;
+      }
+    }
+  } else if (warp == 4) {
+    // ============================================================== MMA
+    if (lane == 0) {
+      uint32_t u = 0;
+      for (int t = 0; t < NB; ++t) {
+        if (!tc_wait(sh.a_full, t & 1, sh, status)) break;
+        tc::fence_after_sync();
+        const int jf = (t + 1 < NB) ? ((64 * (t + 1)) % S) / 256 : 0;
+        bool ok = true;
+        for (int jj = 0; jj < NT && ok; ++jj) {
+          const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
+          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+          const uint32_t idesc =
+              width == 256 ? idesc_full : tc::idesc_bf16(128, width);
+          for (int term = 0; term < T && ok; ++term) {
+            for (int qq = 0; qq < F; ++qq) {
+              const uint32_t slot = u % C::NS;
+              if (!tc_wait(&sh.full[slot], (u / C::NS) & 1, sh, status)) {
+                ok = false;
+                break;
+              }
+              tc::fence_after_sync();
+              const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
+              const uint32_t b0 =
+                  smem_base + (uint32_t)(C::B_OFF + slot * C::B_STAGE);
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks)
+                tc::mma_bf16(taddr + 256 * j,
+                             tc::smem_desc(a0 + 256 * ks, 128, 1024),
+                             tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc, 1u);
+              tc::commit(&sh.free_[slot]);
+              ++u;
+            }
+          }
+          if (jj == 0 && t + 1 < NB) tc::commit(sh.h_ready);
+        }
+        if (!ok) break;
+        tc::commit(sh.mma_done);
+      }
+    }
+  } else {
+    // ========================================================= producer
+    if (lane == 0) {
+      const uint16_t* B = a.tc_b + item.b_off;
+      const float* D = a.tc_diag + item.diag_off;
+      const size_t tile_elems = 256 * 64;
+      auto issue_jbb = [&](int t) {
+        uint64_t* bar = &sh.jbb_full[t & 1];
+        mbar_expect_tx_arrive(bar, 16384);
+        bulk_g2s(smem + C::JBB_OFF + (t & 1) * 16384, D + (size_t)t * 4096,
+                 16384, bar);
+      };
+      if (NB > 0) issue_jbb(0);
+      if (NB > 1) issue_jbb(1);
+      uint32_t u = 0;
+      for (int t = 0; t < NB && !*sh.abort; ++t) {
+        if (t >= 2) {
+          if (!tc_wait(&sh.jbb_free[t & 1], ((t >> 1) - 1) & 1, sh, status))
+            break;
+          issue_jbb(t);
+        }
+        const int jf = (t + 1 < NB) ? ((64 * (t + 1)) % S) / 256 : 0;
+        bool ok = true;
+        for (int jj = 0; jj < NT && ok; ++jj) {
+          const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
+          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+          for (int term = 0; term < T && ok; ++term) {
+            for (int qq = 0; qq < F; ++qq) {
+              const uint32_t slot = u % C::NS;
+              if (u >= (uint32_t)C::NS &&
+                  !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh,
+                           status)) {
+                ok = false;
+                break;
+              }
+              const size_t src =
+                  ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
+              const uint32_t bytes = (uint32_t)width * 128;
+              mbar_expect_tx_arrive(&sh.full[slot], bytes);
+              bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, B + src, bytes,
+                       &sh.full[slot]);
+              ++u;
+            }
+          }
+        }
+        if (!ok) break;
+      }
+    }
+  }
+
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(taddr, ncols);
+  }
+}
+
+// -------------------------------------------------------------- packing
+// B tiles: for block t, term, slice qq, tile j: rows r < width (column
+// qq*S + 256 j + r), k < 64 (spin 64 t + k), canonical no-swizzle K-major
+// order: ((r / 8) * 8 + k / 8) * 64 + (r % 8) * 8 + k % 8 (bf16 elements).
+__global__ void k_pack_tc_b(const float* Jt, int ld, int n, int F, int terms,
+                            uint16_t* out) {
+  const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + 255) / 256;
+  const int64_t tile = 256 * 64;
+  const int64_t total = (int64_t)NB * terms * F * NT * tile;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rest = e;
+    const int within = (int)(rest % tile);
+    rest /= tile;
+    const int j = (int)(rest % NT);
+    rest /= NT;
+    const int qq = (int)(rest % F);
+    rest /= F;
+    const int term = (int)(rest % terms);
+    const int t = (int)(rest / terms);
+    const int cm = within / 64, inside = within % 64;
+    const int r = (cm / 8) * 8 + inside / 8;
+    const int k = (cm % 8) * 8 + inside % 8;
+    const int row = 64 * t + k, col = qq * S + 256 * j + r;
+    float v = 0.0f;
+    if (row < n && col < n && r < 256 && 256 * j + r < S)
+      v = Jt[(int64_t)row * ld + col];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+    const __nv_bfloat16 o = term == 0 ? hi : lo;
+    out[e] = *reinterpret_cast<const uint16_t*>(&o);
+  }
+}
+
+// Diagonal blocks: out[t][k][k2] = J^T[64t + k][64t + k2] (f32).
+__global__ void k_pack_tc_diag(const float* Jt, int ld, int n, float* out) {
+  const int NB = (n + 63) / 64;
+  const int64_t total = (int64_t)NB * 4096;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(e / 4096), k = (int)(e % 4096) / 64, k2 = (int)(e % 64);
+    const int row = 64 * t + k, col = 64 * t + k2;
+    out[e] = (row < n && col < n) ? Jt[(int64_t)row * ld + col] : 0.0f;
+  }
+}
+
+int tc_fold_for(int n) {
+  if (n <= 512) return 1;
+  if (n <= 1024) return 2;
+  if (n <= 2048) return 4;
+  return -1;
+}
+
+int64_t tc_b_elems(int n, int terms) {
+  const int F = tc_fold_for(n);
+  const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + 255) / 256;
+  return (int64_t)NB * terms * F * NT * 256 * 64;
+}
+
+int64_t tc_diag_elems(int n) { return (int64_t)((n + 63) / 64) * 4096; }
+
+cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
+                           uint16_t* b_out, float* diag_out, cudaStream_t st) {
+  const int F = tc_fold_for(n);
+  int64_t tb = tc_b_elems(n, terms);
+  int blocks = (int)((tb + 255) / 256);
+  if (blocks > 8192) blocks = 8192;
+  k_pack_tc_b<<<blocks, 256, 0, st>>>(Jt, ld, n, F, terms, b_out);
+  int64_t td = tc_diag_elems(n);
+  blocks = (int)((td + 255) / 256);
+  if (blocks > 8192) blocks = 8192;
+  k_pack_tc_diag<<<blocks, 256, 0, st>>>(Jt, ld, n, diag_out);
+  return cudaGetLastError();
+}
+
+template <int F>
+static cudaError_t launch_tc_t(const TcArgs& a, int count, cudaStream_t st) {
+  static bool attr_set[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_set[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(
+        k_sweep_tc<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)TcCfg<F>::BYTES);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = true;
+  }
+  k_sweep_tc<F><<<count, 192, TcCfg<F>::BYTES, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc(const TcArgs& a, int F, int count, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  switch (F) {
+    case 1: return launch_tc_t<1>(a, count, st);
+    case 2: return launch_tc_t<2>(a, count, st);
+    case 4: return launch_tc_t<4>(a, count, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+int tc_chains_per_cta(int n) {
+  const int F = tc_fold_for(n);
+  return F > 0 ? 128 / F : 0;
+}
+
+}  // namespace pysa_gb

@@ -41,6 +41,12 @@ def unpack_spins(words_arr: np.ndarray, n: int, problem_type: str,
     return bits.astype(dtype)
 
 
+def bf16_exact(a: np.ndarray) -> bool:
+    """True when every value is exactly representable in bfloat16."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32)
+    return bool(np.all((u & 0xFFFF) == 0))
+
+
 def _ptr(t: torch.Tensor) -> int:
     return t.data_ptr() if t is not None and t.numel() > 0 else 0
 
@@ -57,7 +63,10 @@ class PTBatch:
 
     def __init__(self, problem_type: str, instances: list[Instance],
                  device: torch.device | str | None = None,
-                 perm_slots: int = 1):
+                 perm_slots: int = 1, kernel: str = "auto"):
+        """kernel: 'plain' (CUDA-core sweep), 'tc' (tensor-core blocked
+        sweep, sequential order, 64 <= n <= 2048) or 'auto' (tc when every
+        instance has 256 <= n <= 2048)."""
         if not torch.cuda.is_available():
             raise RuntimeError(
                 "pysa_gb300 needs a CUDA GPU: the sweeps run only as "
@@ -162,6 +171,29 @@ class PTBatch:
         check(self.lib.pysa_gb_setup(ref(self.p), ref(ht_), ref(self.ws),
                                      self._stream.cuda_stream), "setup")
         self._graphs = {}
+        self.tc = False
+        if kernel == "tc" or (kernel == "auto" and I and n.min() >= 256 and
+                              n.max() <= 2048):
+            terms = 1 if all(bf16_exact(x.J) for x in instances) else 2
+            tneed = (ctypes.c_int64 * 3)()
+            titems = check(self.lib.pysa_gb_tc_workspace(I, ref(ht_), terms,
+                                                         tneed), "tc sizing")
+            self.tc_b = z(max(int(tneed[0]), 1), dt=torch.int16)
+            self.tc_diag = z(max(int(tneed[1]), 1), dt=torch.float32)
+            self.tc_items = z(max(int(tneed[2]), 8), dt=torch.int32)
+            self.ws.tc_b = _ptr(self.tc_b)
+            self.ws.tc_b_elems = int(tneed[0])
+            self.ws.tc_diag = _ptr(self.tc_diag)
+            self.ws.tc_diag_elems = int(tneed[1])
+            self.ws.tc_items = _ptr(self.tc_items)
+            self.ws.tc_num_items = max(titems, 1)
+            self.ws.tc_terms = terms
+            check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(ht_),
+                                            ref(self.ws),
+                                            self._stream.cuda_stream),
+                  "tc setup")
+            self.tc = True
+            self.tc_terms = terms
 
     # ------------------------------------------------------------ states
     def set_states(self, spins_words: np.ndarray, energies=None,
