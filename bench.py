@@ -191,7 +191,7 @@ def run_reference_arm(args, w, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="qubo1024", choices=list(WORKLOADS))
@@ -223,7 +223,8 @@ def main():
     J = P.copy()
     np.fill_diagonal(J, 0)
     R, Rd, n = w["replicas"], w["reads"], w["n"]
-    batch = PTBatch(ptype, [Instance(J, h, ladder(w), Rd)])
+    batch = PTBatch(ptype, [Instance(J, h, ladder(w), Rd)], kernel="auto")
+    use_tc = batch.tc and w["update"] == "sequential"
     rng = np.random.default_rng(100 + rank)
     if ptype == "qubo":
         x0 = rng.integers(0, 2, (Rd, R, n)).astype(np.float32)
@@ -233,8 +234,10 @@ def main():
     upd = _lib.RANDOM if w["update"] == "random" else _lib.SEQUENTIAL
     seed = 7 + rank
 
+    rc_every = 4 if (use_tc and batch.tc_terms == 2) else 0
+
     def opts(phases):
-        return _lib.Options(seed, upd, 1, 0, 0, phases, 0)
+        return _lib.Options(seed, upd, 1, 0, 0, phases, rc_every)
 
     stream = torch.cuda.current_stream()
     st = stream.cuda_stream
@@ -278,18 +281,62 @@ def main():
     attempts_per_step = Rd * R * n
     value = attempts_per_step * args.steps * world / total_s
 
-    # roofline of the sweep kernel: algorithmic bytes of one launch =
-    # fields read+write + spins read+write + J once
+    # plain CUDA-core sweep on the same chains, for comparison
+    plain = None
+    if use_tc:
+        pb = PTBatch(ptype, [Instance(J, h, ladder(w), Rd)], kernel="plain")
+        pb.set_states(pack_spins(x0, ptype, pb.words), None)
+        po = _lib.Options(seed, upd, 1, 0, 0, 1, 0)
+        for _ in range(3):
+            check(lib.pysa_gb_sweeps(ref(pb.p), ref(pb.s), ref(pb.ws),
+                                     ref(po), 1, st), "plain warm-up")
+        pk = min(args.steps, 30)
+        pev = [(torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True)) for _ in range(pk)]
+        for a_, b_ in pev:
+            flush.fill_(1.0)
+            a_.record(stream)
+            check(lib.pysa_gb_sweeps(ref(pb.p), ref(pb.s), ref(pb.ws),
+                                     ref(po), 1, st), "plain sweep")
+            b_.record(stream)
+        torch.cuda.synchronize()
+        pms = float(np.mean([a_.elapsed_time(b_) for a_, b_ in pev]))
+        plain = {"kernel": "k_sweep_plain<32,4,8,8>", "sweep_ms": pms,
+                 "value": Rd * R * n / (pms / 1e3), "unit": "attempts/s",
+                 "steps": pk}
+        del pb
+
     C = Rd * R
-    alg_bytes = C * (2 * 4 * n + 2 * 4 * batch.words + 16) + 4 * n * n
     sweep_s = np.mean(sweep_ms) / 1e3
     hbm, bf16, peak_kind = measured_peaks()
-    achieved = alg_bytes / sweep_s / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "sweep_plain_qubo1024_traffic.json")
+    if use_tc:
+        # algorithmic tensor work of one sweep launch: the rank-64 field
+        # updates H += A B over every block, 2 C n^2 FLOP per BF16 term
+        terms = batch.tc_terms
+        alg = 2.0 * C * n * n * terms
+        fold = 1 if n <= 512 else (2 if n <= 1024 else 4)
+        roof = {"bound": "tensor", "achieved": alg / sweep_s / 1e12,
+                "peak": bf16, "unit": "TFLOP/s",
+                "frac": alg / sweep_s / 1e12 / bf16, "traffic": None,
+                "peak_source": peak_kind + " (bf16 burst)",
+                "kernel": f"k_sweep_tc<{fold}>", "bf16_terms": terms,
+                "issued_flop_per_launch": alg * fold,
+                "alg_flop_per_launch": alg, "sweep_ms": sweep_s * 1e3}
+        tp = os.path.join(ROOT, "profiles", "sweep_tc_qubo1024_traffic.json")
+    else:
+        # algorithmic bytes of one launch: fields read+write, spins
+        # read+write, J once
+        alg_bytes = C * (2 * 4 * n + 2 * 4 * batch.words + 16) + 4 * n * n
+        roof = {"bound": "hbm", "achieved": alg_bytes / sweep_s / 1e9,
+                "peak": hbm, "unit": "GB/s",
+                "frac": alg_bytes / sweep_s / 1e9 / hbm, "traffic": None,
+                "peak_source": peak_kind, "kernel": "k_sweep_plain<32,4,8,8>",
+                "alg_bytes_per_launch": int(alg_bytes),
+                "sweep_ms": sweep_s * 1e3}
+        tp = os.path.join(ROOT, "profiles", "sweep_plain_qubo1024_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+            roof["traffic"] = json.load(f).get("bytes_per_launch")
 
     # end to end through the public API (host buffers in and out)
     e2e = None
@@ -315,8 +362,10 @@ def main():
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
-        reads_cpu = 8
-        sweeps_cpu = 5
+        reads_cpu = 16
+        rate, dt = cpu_reference(w, ptype, P, reads_cpu, 2)
+        # size the sample to about 15 s of CPU work
+        sweeps_cpu = max(2, int(2 * 15.0 / max(dt, 1e-3)))
         rate, dt = cpu_reference(w, ptype, P, reads_cpu, sweeps_cpu)
         cpu = {"value": rate, "unit": "attempts/s",
                "cores": os.cpu_count() or 1, "kind": "port",
@@ -336,13 +385,11 @@ def main():
                        "reads": Rd, "chains": C, "update": w["update"],
                        "exchange": "every sweep", "problem": w["kind"],
                        "l2": "flushed (256 MB write) before every step",
-                       "kernel": "plain local-field sweep (CUDA cores)"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
-                         "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_sweep_plain<32,4,8,8>",
-                         "sweep_ms": float(np.mean(sweep_ms)),
-                         "alg_bytes_per_launch": int(alg_bytes)},
+                       "kernel": ("tensor-core blocked sweep (tcgen05, "
+                                  "split-BF16)") if use_tc else
+                                 "plain local-field sweep (CUDA cores)"},
+            "roofline": roof,
+            "plain_gpu": plain,
             "clocks": sampler.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,

@@ -151,7 +151,9 @@ typedef struct {
                               1: energies start at +inf best (sequential) */
   int32_t phases;          /* 0 = all; bit 0: visiting order + sweep kernel,
                               bit 1: exchange (lets a caller time each) */
-  int32_t pad_;
+  int32_t recompute_every; /* tensor-core sweep: rebuild fields and energies
+                              from the spins at the start of every sweep whose
+                              index is a multiple of this (0 = never) */
 } pysa_gb_options;
 
 /* ABI version (PYSA_GB_ABI_VERSION) and the last error of this thread. */

@@ -55,7 +55,7 @@ class HostTables(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("seed", U64), ("update", I32), ("use_pt", I32),
                 ("log_omega_stride", I32), ("best_global", I32),
-                ("phases", I32), ("pad_", I32)]
+                ("phases", I32), ("recompute_every", I32)]
 
 
 class AisOptions(ctypes.Structure):

@@ -349,6 +349,8 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.tc_b = ws->tc_b;
   ta.tc_diag = ws->tc_diag;
   ta.seed = o->seed;
+  ta.recompute_every = o->recompute_every;
+  ta.pad_ = 0;
   for (int sw = 0; sw < num_sweeps; ++sw) {
     if (use_tc && (phases & 1)) {
       const int folds[3] = {1, 2, 4};

@@ -42,16 +42,20 @@ struct TcCfg {
   static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
   static constexpr size_t SPIN_OFF = JBB_OFF + 2 * 16384;
   static constexpr size_t DE_OFF = SPIN_OFF + (size_t)CC * WORDS * 4;
-  static constexpr size_t BETA_OFF = DE_OFF + (size_t)CC * 8;
+  static constexpr size_t E0_OFF = DE_OFF + (size_t)CC * 8;
+  static constexpr size_t EPART_OFF = E0_OFF + (size_t)CC * 8;
+  static constexpr size_t BETA_OFF = EPART_OFF + (size_t)F * CC * 8;
   static constexpr size_t BAR_OFF = (BETA_OFF + CC * 4 + 63) / 64 * 64;
-  // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], full[NS], free[NS]
-  static constexpr int NBARS = 7 + 2 * NS;
+  // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
+  // full[NS], free[NS]
+  static constexpr int NBARS = 9 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
   static constexpr size_t BYTES = MISC_OFF + 16;
 };
 
 struct TcShared {
-  uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *full, *free_;
+  uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *rc_full,
+      *rc_done, *full, *free_;
   uint32_t* tmem_slot;
   volatile int32_t* abort;
 };
@@ -92,12 +96,16 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   sh.h_ready = bars + 2;
   sh.jbb_full = bars + 3;
   sh.jbb_free = bars + 5;
-  sh.full = bars + 7;
-  sh.free_ = bars + 7 + C::NS;
+  sh.rc_full = bars + 7;
+  sh.rc_done = bars + 8;
+  sh.full = bars + 9;
+  sh.free_ = bars + 9 + C::NS;
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
   uint32_t* spins_s = reinterpret_cast<uint32_t*>(smem + C::SPIN_OFF);
   double* dE_s = reinterpret_cast<double*>(smem + C::DE_OFF);
+  double* e0_s = reinterpret_cast<double*>(smem + C::E0_OFF);
+  double* epart_s = reinterpret_cast<double*>(smem + C::EPART_OFF);
   float* beta_s = reinterpret_cast<float*>(smem + C::BETA_OFF);
   const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
   const uint32_t smem_base = smem_addr(smem);
@@ -118,6 +126,9 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   const int64_t chain_base = a.p.chain_off[inst];
   uint32_t ncols = 32;
   while (ncols < (uint32_t)S) ncols <<= 1;
+  // recompute H = J s + h and E on the tensor cores at the start of this
+  // sweep (bounds the FP32 accumulator drift of the split-BF16 path)
+  const bool rc = a.recompute_every > 0 && (sweep % a.recompute_every) == 0;
 
   // ---------------------------------------------------------------- set-up
   if (warp == 0) {
@@ -139,6 +150,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   }
   for (int c = threadIdx.x; c < CC; c += blockDim.x) {
     dE_s[c] = 0.0;
+    e0_s[c] = c < item.nchains ? (double)a.s.energies[item.chain0 + c] : 0.0;
     beta_s[c] = c < item.nchains ? a.s.chain_beta[item.chain0 + c] : 0.0f;
   }
   fence_proxy_async();
@@ -154,7 +166,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   const int64_t chain = item.chain0 + c;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 
-  if (warp < 4) {  // local fields -> TMEM
+  if (warp < 4 && !rc) {  // local fields -> TMEM
     for (int j0 = 0; j0 < S; j0 += 32) {
       float v[32];
       const float* f = a.fields + chain * a.field_ld + q * S + j0;
@@ -170,6 +182,77 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   tc::fence_after_sync();
 
   const uint32_t idesc_full = tc::idesc_bf16(128, 256);
+
+  if (warp < 4 && rc) {
+    // ================================================ recompute: A = spins
+    for (int t = 0; t < NB; ++t) {
+      bool go = q == 0 && !*sh.abort;
+      if (go && t > 0) go = tc_wait(sh.rc_done, (t - 1) & 1, sh, status);
+      if (go) {
+        const uint32_t w0 = spins_s[(2 * t) * CC + c];
+        const uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
+        const int kmax = n - 64 * t < 64 ? n - 64 * t : 64;
+        uint32_t pk[32];
+#pragma unroll
+        for (int k = 0; k < 64; ++k) {
+          const bool sb = k < 32 ? ((w0 >> k) & 1u) : ((w1 >> (k - 32)) & 1u);
+          const float v = (!valid || k >= kmax) ? 0.0f
+                          : sb ? 1.0f : (ising ? -1.0f : 0.0f);
+          const uint32_t b16 = bf16_bits(v);
+          if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
+        }
+#pragma unroll
+        for (int qq = 0; qq < F; ++qq) {
+          const int m = qq * CC + c;
+          unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                ((m >> 3) * 8) * 128 + (m & 7) * 16;
+#pragma unroll
+          for (int kc = 0; kc < 8; ++kc)
+            *reinterpret_cast<uint4*>(rowp + kc * 128) =
+                make_uint4(pk[4 * kc], pk[4 * kc + 1], pk[4 * kc + 2],
+                           pk[4 * kc + 3]);
+        }
+        fence_proxy_async();
+      }
+      named_sync_128();
+      if (threadIdx.x == 0) mbar_arrive(sh.rc_full);
+    }
+    if (!*sh.abort && NB > 0) tc_wait(sh.rc_done, (NB - 1) & 1, sh, status);
+    tc::fence_after_sync();
+    // H = J s + h in TMEM; partial energies sum_j s_j ((J s)_j / 2 + h_j)
+    const float* hh = a.p.h + a.p.h_off[inst];
+    double ep = 0.0;
+    if (!*sh.abort) {
+      for (int j0 = 0; j0 < S; j0 += 32) {
+        float v[32];
+        tc::tmem_ld32(taddr + lane_base + j0, v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int col = q * S + j0 + i;
+          if (col < n) {
+            const uint32_t wv = spins_s[(col >> 5) * CC + c];
+            const double sj =
+                ((wv >> (col & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+            const float hj = hh[col];
+            ep += sj * (0.5 * (double)v[i] + (double)hj);
+            v[i] = v[i] + hj;
+          }
+        }
+        tc::tmem_st32(taddr + lane_base + j0, v);
+      }
+      tc::tmem_wait_st();
+    }
+    epart_s[q * CC + c] = ep;
+    tc::fence_before_sync();
+    named_sync_128();
+    tc::fence_after_sync();
+    if (q == 0 && valid) {
+      double e = 0.0;
+      for (int qq = 0; qq < F; ++qq) e += epart_s[qq * CC + c];
+      e0_s[c] = (double)(float)e;
+    }
+    named_sync_128();
+  }
 
   if (warp < 4) {
     // ============================================================ decide
@@ -269,7 +352,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
     tc::fence_before_sync();
     named_sync_128();
     if (q == 0 && valid && !*sh.abort) {
-      const float e_new = (float)((double)a.s.energies[chain] + dE_s[c]);
+      const float e_new = (float)(e0_s[c] + dE_s[c]);
       a.s.energies[chain] = e_new;
       const bool improved = e_new < a.s.best_energy[chain];
       if (improved) {
@@ -286,6 +369,39 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
     // ============================================================== MMA
     if (lane == 0) {
       uint32_t u = 0;
+      for (int t = 0; rc && t < NB; ++t) {
+        if (!tc_wait(sh.rc_full, t & 1, sh, status)) break;
+        tc::fence_after_sync();
+        bool ok = true;
+        for (int j = 0; j < NT && ok; ++j) {
+          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+          const uint32_t idesc =
+              width == 256 ? idesc_full : tc::idesc_bf16(128, width);
+          for (int term = 0; term < T && ok; ++term) {
+            for (int qq = 0; qq < F; ++qq) {
+              const uint32_t slot = u % C::NS;
+              if (!tc_wait(&sh.full[slot], (u / C::NS) & 1, sh, status)) {
+                ok = false;
+                break;
+              }
+              tc::fence_after_sync();
+              const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
+              const uint32_t b0 =
+                  smem_base + (uint32_t)(C::B_OFF + slot * C::B_STAGE);
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks)
+                tc::mma_bf16(taddr + 256 * j,
+                             tc::smem_desc(a0 + 256 * ks, 128, 1024),
+                             tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc,
+                             (t | term | qq | ks) ? 1u : 0u);
+              tc::commit(&sh.free_[slot]);
+              ++u;
+            }
+          }
+        }
+        if (!ok) break;
+        tc::commit(sh.rc_done);
+      }
       for (int t = 0; t < NB; ++t) {
         if (!tc_wait(sh.a_full, t & 1, sh, status)) break;
         tc::fence_after_sync();
@@ -337,6 +453,31 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
       if (NB > 0) issue_jbb(0);
       if (NB > 1) issue_jbb(1);
       uint32_t u = 0;
+      for (int t = 0; rc && t < NB && !*sh.abort; ++t) {
+        bool ok = true;
+        for (int j = 0; j < NT && ok; ++j) {
+          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+          for (int term = 0; term < T && ok; ++term) {
+            for (int qq = 0; qq < F; ++qq) {
+              const uint32_t slot = u % C::NS;
+              if (u >= (uint32_t)C::NS &&
+                  !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh,
+                           status)) {
+                ok = false;
+                break;
+              }
+              const size_t src =
+                  ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
+              const uint32_t bytes = (uint32_t)width * 128;
+              mbar_expect_tx_arrive(&sh.full[slot], bytes);
+              bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, B + src, bytes,
+                       &sh.full[slot]);
+              ++u;
+            }
+          }
+        }
+        if (!ok) break;
+      }
       for (int t = 0; t < NB && !*sh.abort; ++t) {
         if (t >= 2) {
           if (!tc_wait(&sh.jbb_free[t & 1], ((t >> 1) - 1) & 1, sh, status))

@@ -24,6 +24,8 @@ struct TcArgs {
   const float* tc_diag;
   const TcItem* items;
   uint64_t seed;
+  int32_t recompute_every;  // >0: H and E rebuilt when sweep % this == 0
+  int32_t pad_;
 };
 
 int tc_fold_for(int n);  // 1, 2, 4 or -1 (n > 2048)

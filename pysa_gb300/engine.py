@@ -223,7 +223,13 @@ class PTBatch:
     # ------------------------------------------------------------ sweeps
     def run(self, num_sweeps: int, *, seed: int, update: str = "sequential",
             use_pt: bool = True, log_omega: bool = False,
-            graph_chunk: int = 64):
+            graph_chunk: int = 64, recompute_every: int | None = None):
+        """Sweeps with exchange.  recompute_every: the tensor-core path
+        rebuilds fields and energies from the spins every that many sweeps
+        (default 4 when J is not exact in BF16, never otherwise); the
+        returned energies are then recomputed once more at the end."""
+        if recompute_every is None:
+            recompute_every = 4 if (self.tc and self.tc_terms == 2) else 0
         upd = _lib.RANDOM if update == "random" else _lib.SEQUENTIAL
         stride = int(num_sweeps) if log_omega else 0
         if log_omega:
@@ -234,7 +240,7 @@ class PTBatch:
         else:
             self.s.log_omega = 0
         opts = _lib.Options(seed & ((1 << 64) - 1), upd, int(use_pt), stride,
-                            int(self.best_global), 0, 0)
+                            int(self.best_global), 0, int(recompute_every))
         st = self._stream.cuda_stream
         # first call with zero sweeps sets kernel attributes outside capture
         check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s), ref(self.ws),
@@ -256,6 +262,12 @@ class PTBatch:
             check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s),
                                           ref(self.ws), ref(opts), remaining,
                                           st), "sweeps")
+        if recompute_every and upd == _lib.SEQUENTIAL and self.tc:
+            # final fields and energies from the spins (f64-accumulated)
+            check(self.lib.pysa_gb_prepare(ref(self.p), ref(self.s),
+                                           ref(self.ws), 1, 0,
+                                           int(self.best_global), st),
+                  "final recompute")
 
     def check_status(self):
         code = int(self.status.item())
