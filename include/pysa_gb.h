@@ -160,6 +160,13 @@ typedef struct {
 int pysa_gb_abi_version(void);
 const char *pysa_gb_last_error(void);
 
+/* Diagnostics: when `device_buffer` (>= 8 x 64 uint64) is not NULL, the
+ * tensor-core sweep records a per-block globaltimer timeline of its first CTA
+ * there (decision start, fields loaded, decisions done, A free, A published,
+ * MMA start, next-block fields committed, stages issued).  NULL turns it off.
+ * No counterpart in the reference. */
+int pysa_gb_set_trace(void *device_buffer);
+
 /* Workspace sizing and set-up.
  *   pysa_gb_workspace_bytes: sizes of the workspace arrays for a batch
  *     described by host tables (n, replicas, reads are read); returns the

@@ -36,6 +36,7 @@ static int row_floats(int v) {
 static int lane_stride(int v) { return row_floats(v) / 32; }
 
 static thread_local std::string g_last_error;
+static unsigned long long* g_tc_trace = nullptr;  // diagnostics, see below
 
 static int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -89,6 +90,11 @@ using namespace pysa_gb;
 extern "C" {
 
 int pysa_gb_abi_version(void) { return PYSA_GB_ABI_VERSION; }
+
+int pysa_gb_set_trace(void* device_buffer) {
+  g_tc_trace = reinterpret_cast<unsigned long long*>(device_buffer);
+  return PYSA_GB_OK;
+}
 
 const char* pysa_gb_last_error(void) { return g_last_error.c_str(); }
 
@@ -351,6 +357,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.seed = o->seed;
   ta.recompute_every = o->recompute_every;
   ta.pad_ = 0;
+  ta.trace = g_tc_trace;
   for (int sw = 0; sw < num_sweeps; ++sw) {
     if (use_tc && (phases & 1)) {
       const int folds[3] = {1, 2, 4};

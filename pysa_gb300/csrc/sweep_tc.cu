@@ -75,6 +75,11 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
   }
 }
 
+// Timeline stamp of CTA 0 when a trace buffer is given (diagnostics only).
+__device__ __forceinline__ void stamp(const TcArgs& a, int t, int slot) {
+  if (a.trace && blockIdx.x == 0) a.trace[t * 8 + slot] = globaltimer_ns();
+}
+
 __device__ __forceinline__ void named_sync_128() {
   asm volatile("bar.sync 1, 128;" ::: "memory");
 }
@@ -267,11 +272,14 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
       bool go = q == qt && !*sh.abort;
       if (go && t > 0) go = tc_wait(sh.h_ready, (t - 1) & 1, sh, status);
       if (go) go = tc_wait(&sh.jbb_full[t & 1], (t >> 1) & 1, sh, status);
+      const bool lead = go && c == 0;
+      if (lead) stamp(a, t, 0);
       if (go) {
         tc::fence_after_sync();
         float h[64];
         tc::tmem_ld32(taddr + lane_base + co, h);
         tc::tmem_ld32(taddr + lane_base + co + 32, h + 32);
+        if (lead) stamp(a, t, 1);
         const float4* jb4 = reinterpret_cast<const float4*>(jbb + (t & 1) * 4096);
         uint32_t w0 = spins_s[(2 * t) * CC + c];
         uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
@@ -311,9 +319,11 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
           spins_s[(2 * t + 1) * CC + c] = w1;
           dE_s[c] += (double)dEb;
         }
+        if (lead) stamp(a, t, 2);
         // A is single-buffered: the previous block's MMAs must be done
         const bool a_free =
             t == 0 || tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
+        if (lead) stamp(a, t, 3);
 #pragma unroll
         for (int qq = 0; qq < F && a_free; ++qq) {
           const int m = qq * CC + c;  // A row = TMEM lane of (slice qq, chain c)
@@ -329,6 +339,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
       }
       named_sync_128();
       if (threadIdx.x == 0) {
+        stamp(a, t, 4);
         mbar_arrive(sh.a_full);
         mbar_arrive(&sh.jbb_free[t & 1]);
       }
@@ -404,6 +415,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
       }
       for (int t = 0; t < NB; ++t) {
         if (!tc_wait(sh.a_full, t & 1, sh, status)) break;
+        stamp(a, t, 5);
         tc::fence_after_sync();
         const int jf = (t + 1 < NB) ? ((64 * (t + 1)) % S) / 256 : 0;
         bool ok = true;
@@ -432,7 +444,10 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
               ++u;
             }
           }
-          if (jj == 0 && t + 1 < NB) tc::commit(sh.h_ready);
+          if (jj == 0 && t + 1 < NB) {
+            tc::commit(sh.h_ready);
+            stamp(a, t, 6);
+          }
         }
         if (!ok) break;
         tc::commit(sh.mma_done);
@@ -509,6 +524,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
           }
         }
         if (!ok) break;
+        stamp(a, t, 7);
       }
     }
   }

@@ -26,6 +26,8 @@ struct TcArgs {
   uint64_t seed;
   int32_t recompute_every;  // >0: H and E rebuilt when sweep % this == 0
   int32_t pad_;
+  // optional timeline of CTA 0 (globaltimer ns): [block][8] stamps
+  unsigned long long* trace;
 };
 
 int tc_fold_for(int n);  // 1, 2, 4 or -1 (n > 2048)
