@@ -160,11 +160,12 @@ typedef struct {
 int pysa_gb_abi_version(void);
 const char *pysa_gb_last_error(void);
 
-/* Diagnostics: when `device_buffer` (>= 8 x 64 uint64) is not NULL, the
+/* Diagnostics: when `device_buffer` (>= 24 x 64 uint64) is not NULL, the
  * tensor-core sweep records a per-block globaltimer timeline of its first CTA
- * there (decision start, fields loaded, decisions done, A free, A published,
- * MMA start, next-block fields committed, stages issued).  NULL turns it off.
- * No counterpart in the reference. */
+ * there: [0] decision start, [1] fields ready, [2] decisions done, [3] A free,
+ * [4] A published, [5] MMA start, [6] next-block fields committed, [7] stages
+ * issued, [8 + 3g .. 10 + 3g] sub-block g: fields loaded, lazy corrections
+ * applied, decided.  NULL turns it off.  No counterpart in the reference. */
 int pysa_gb_set_trace(void *device_buffer);
 
 /* Workspace sizing and set-up.

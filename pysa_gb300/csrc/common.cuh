@@ -70,6 +70,16 @@ __device__ __forceinline__ double uniform64(uint32_t x) {
 // Fast path: lf = __logf(u32) has absolute error < 1e-5 over u in (0,1); the
 // f32 product beta*dn has relative error < 2^-23.  Outside that band the f32
 // comparison already gives the exact answer; inside it the f64 rule decides.
+// The f64 rule is kept out of line: if-converted into the hot loop it would
+// issue its FP64 instructions (a slow pipe on this part) on every decision.
+static __device__ __noinline__ bool accept_slow(float dn, float beta, uint32_t x) {
+  return log(uniform64(x)) < (double)beta * (double)dn;
+}
+
+static __device__ __noinline__ bool accept_full_slow(double full, uint32_t x) {
+  return log(uniform64(x)) < full;
+}
+
 __device__ __forceinline__ bool metropolis_accept(float dn, float beta,
                                                   uint32_t x) {
   if (dn >= 0.0f) return true;
@@ -80,7 +90,40 @@ __device__ __forceinline__ bool metropolis_accept(float dn, float beta,
   const float margin = 3e-5f + 1e-6f * fabsf(bd);
   if (lf < bd - margin) return true;
   if (lf > bd + margin) return false;
+  return accept_slow(dn, beta, x);
+}
+
+// Same rule with log(u) precomputed in f32 (lf = __logf of the f32 uniform,
+// bit-identical to the value metropolis_accept forms); the rare exact f64
+// decision redraws x from the stream.
+static __device__ __noinline__ bool accept_slow_redraw(float dn, float beta,
+                                                       uint64_t seed,
+                                                       uint32_t inst,
+                                                       uint32_t sweep,
+                                                       uint32_t chain,
+                                                       uint32_t step) {
+  uint32_t o[4];
+  philox4x32_10(step >> 2, sweep, chain, (inst << 4) | TAG_SWEEP,
+                (uint32_t)seed, (uint32_t)(seed >> 32), o);
+  const uint32_t k = step & 3;
+  const uint32_t x = k == 0 ? o[0] : k == 1 ? o[1] : k == 2 ? o[2] : o[3];
   return log(uniform64(x)) < (double)beta * (double)dn;
+}
+
+__device__ __forceinline__ float log_uniform_f32(uint32_t x) {
+  return __logf(__uint2float_rn(x) * 0x1p-32f + 0x1p-33f);
+}
+
+__device__ __forceinline__ bool metropolis_accept_lf(
+    float dn, float beta, float lf, uint64_t seed, uint32_t inst,
+    uint32_t sweep, uint32_t chain, uint32_t step) {
+  if (dn >= 0.0f) return true;
+  const float bd = beta * dn;
+  if (bd < -24.0f) return false;
+  const float margin = 3e-5f + 1e-6f * fabsf(bd);
+  if (lf < bd - margin) return true;
+  if (lf > bd + margin) return false;
+  return accept_slow_redraw(dn, beta, seed, inst, sweep, chain, step);
 }
 
 // Same rule on a precomputed f64 threshold (AIS form: full >= 0 accepts).
@@ -93,7 +136,7 @@ __device__ __forceinline__ bool accept_full(double full, uint32_t x) {
   const float margin = 3e-5f + 1e-6f * fabsf(ff);
   if (lf < ff - margin) return true;
   if (lf > ff + margin) return false;
-  return log(uniform64(x)) < full;
+  return accept_full_slow(full, x);
 }
 
 // ------------------------------------------------------------ status word

@@ -22,7 +22,7 @@
 // exact, so trajectories match the plain sweep bit for bit.
 //
 // Roles: warps 0-3 decide (thread = TMEM lane), warp 4 issues MMAs, warp 5
-// produces stages.  Every wait is bounded; a timeout sets the status word and
+// produces stages, warps 6-7 precompute the next block's log-uniforms.  Every wait is bounded; a timeout sets the status word and
 // an abort flag that releases every other wait.
 #include "aux.cuh"
 #include "tc_api.h"
@@ -33,7 +33,7 @@ namespace pysa_gb {
 template <int F>
 struct TcCfg {
   static constexpr int CC = 128 / F;          // chains per CTA
-  static constexpr int NS = F == 4 ? 3 : 4;   // B ring stages
+  static constexpr int NS = F == 1 ? 2 : 3;   // B ring stages
   static constexpr int WORDS = 16 * F;        // spin words per chain
   static constexpr size_t A_OFF = 0;
   static constexpr size_t A_BYTES = (size_t)F * 16384;
@@ -41,21 +41,24 @@ struct TcCfg {
   static constexpr size_t B_STAGE = 32768;
   static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
   static constexpr size_t SPIN_OFF = JBB_OFF + 2 * 16384;
-  static constexpr size_t DE_OFF = SPIN_OFF + (size_t)CC * WORDS * 4;
+  static constexpr size_t LF_OFF = SPIN_OFF + (size_t)CC * WORDS * 4;
+  static constexpr size_t DL_OFF = LF_OFF + (size_t)2 * 64 * CC * 4;
+  static constexpr size_t DE_OFF = DL_OFF + (size_t)64 * CC * 4;
   static constexpr size_t E0_OFF = DE_OFF + (size_t)CC * 8;
   static constexpr size_t EPART_OFF = E0_OFF + (size_t)CC * 8;
   static constexpr size_t BETA_OFF = EPART_OFF + (size_t)F * CC * 8;
   static constexpr size_t BAR_OFF = (BETA_OFF + CC * 4 + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
-  // full[NS], free[NS]
-  static constexpr int NBARS = 9 + 2 * NS;
+  // lf_full[2], lf_free[2], full[NS], free[NS]
+  static constexpr int NBARS = 13 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
   static constexpr size_t BYTES = MISC_OFF + 16;
+  static_assert(BYTES <= 232448, "shared memory budget");
 };
 
 struct TcShared {
   uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *rc_full,
-      *rc_done, *full, *free_;
+      *rc_done, *lf_full, *lf_free, *full, *free_;
   uint32_t* tmem_slot;
   volatile int32_t* abort;
 };
@@ -77,11 +80,20 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
 
 // Timeline stamp of CTA 0 when a trace buffer is given (diagnostics only).
 __device__ __forceinline__ void stamp(const TcArgs& a, int t, int slot) {
-  if (a.trace && blockIdx.x == 0) a.trace[t * 8 + slot] = globaltimer_ns();
+  if (a.trace && blockIdx.x == 0) a.trace[t * 24 + slot] = globaltimer_ns();
 }
 
+// Named barriers in inline PTX: the warp is reconverged first and the
+// non-aligned barrier.sync form is used, since the compiler does not insert
+// the reconvergence it adds before __syncthreads().
 __device__ __forceinline__ void named_sync_128() {
-  asm volatile("bar.sync 1, 128;" ::: "memory");
+  __syncwarp();
+  asm volatile("barrier.sync 1, 128;" ::: "memory");
+}
+
+__device__ __forceinline__ void named_sync_helpers() {
+  __syncwarp();
+  asm volatile("barrier.sync 2, 64;" ::: "memory");
 }
 
 __device__ __forceinline__ uint32_t bf16_bits(float d) {
@@ -90,7 +102,7 @@ __device__ __forceinline__ uint32_t bf16_bits(float d) {
 }
 
 template <int F>
-__global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
+__global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   using C = TcCfg<F>;
   constexpr int CC = C::CC;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -103,8 +115,10 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   sh.jbb_free = bars + 5;
   sh.rc_full = bars + 7;
   sh.rc_done = bars + 8;
-  sh.full = bars + 9;
-  sh.free_ = bars + 9 + C::NS;
+  sh.lf_full = bars + 9;
+  sh.lf_free = bars + 11;
+  sh.full = bars + 13;
+  sh.free_ = bars + 13 + C::NS;
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
   uint32_t* spins_s = reinterpret_cast<uint32_t*>(smem + C::SPIN_OFF);
@@ -113,6 +127,8 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
   double* epart_s = reinterpret_cast<double*>(smem + C::EPART_OFF);
   float* beta_s = reinterpret_cast<float*>(smem + C::BETA_OFF);
   const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
+  float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
+  float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
   const uint32_t smem_base = smem_addr(smem);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -193,6 +209,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
     for (int t = 0; t < NB; ++t) {
       bool go = q == 0 && !*sh.abort;
       if (go && t > 0) go = tc_wait(sh.rc_done, (t - 1) & 1, sh, status);
+      go = __all_sync(0xffffffffu, go);
       if (go) {
         const uint32_t w0 = spins_s[(2 * t) * CC + c];
         const uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
@@ -227,7 +244,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
     // H = J s + h in TMEM; partial energies sum_j s_j ((J s)_j / 2 + h_j)
     const float* hh = a.p.h + a.p.h_off[inst];
     double ep = 0.0;
-    if (!*sh.abort) {
+    if (__all_sync(0xffffffffu, !*sh.abort)) {
       for (int j0 = 0; j0 < S; j0 += 32) {
         float v[32];
         tc::tmem_ld32(taddr + lane_base + j0, v);
@@ -272,83 +289,175 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
       bool go = q == qt && !*sh.abort;
       if (go && t > 0) go = tc_wait(sh.h_ready, (t - 1) & 1, sh, status);
       if (go) go = tc_wait(&sh.jbb_full[t & 1], (t >> 1) & 1, sh, status);
+      if (go) go = tc_wait(&sh.lf_full[t & 1], (t >> 1) & 1, sh, status);
+      // warp-uniform, so the warp-collective TMEM loads below stay converged
+      go = __all_sync(0xffffffffu, go);
       const bool lead = go && c == 0;
       if (lead) stamp(a, t, 0);
       if (go) {
         tc::fence_after_sync();
-        float h[64];
-        tc::tmem_ld32(taddr + lane_base + co, h);
-        tc::tmem_ld32(taddr + lane_base + co + 32, h + 32);
         if (lead) stamp(a, t, 1);
-        const float4* jb4 = reinterpret_cast<const float4*>(jbb + (t & 1) * 4096);
-        uint32_t w0 = spins_s[(2 * t) * CC + c];
-        uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
+        const float* jb = jbb + (t & 1) * 4096;
+        const float* lfb = lf_s + (t & 1) * 64 * CC;
+        const uint32_t o0 = spins_s[(2 * t) * CC + c];
+        const uint32_t o1 = spins_s[(2 * t + 1) * CC + c];
+        uint32_t w0 = o0, w1 = o1;
         float dEb = 0.0f;
-        uint32_t pk[32];  // bf16 pairs of the 64 deltas
-        uint32_t x4[4];
+        bool a_ok = true;
+        // four sub-blocks of 16 spins; corrections from earlier sub-blocks
+        // are applied lazily when a sub-block's fields are loaded
+#pragma unroll 1
+        for (int g = 0; g < 4; ++g) {
+          float hs[16];
+          tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
+          if (lead) stamp(a, t, 8 + 3 * g);
+#pragma unroll 2
+          for (int k = 0; k < 16 * g; ++k) {
+            const float d = dl_s[k * CC + c];
+            const float4* jr =
+                reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
 #pragma unroll
-        for (int k = 0; k < 64; ++k) {
-          if ((k & 3) == 0)
-            draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, chain_local,
-                  (uint32_t)((i0 + k) >> 2), x4);
-          const bool s = k < 32 ? ((w0 >> k) & 1u) : ((w1 >> (k - 32)) & 1u);
-          const float hk = h[k];
-          const float dn = ising ? (s ? 2.0f * hk : -2.0f * hk) : (s ? hk : -hk);
-          const bool acc = valid && k < kmax &&
-                           metropolis_accept(dn, beta, x4[k & 3]);
-          const float dl =
-              acc ? (ising ? (s ? -2.0f : 2.0f) : (s ? -1.0f : 1.0f)) : 0.0f;
-          if (acc) {
-            dEb -= dn;
-            if (k < 32) w0 ^= 1u << k; else w1 ^= 1u << (k - 32);
+            for (int q4 = 0; q4 < 4; ++q4) {
+              const float4 v = jr[q4];
+              hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
+              hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
+              hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
+              hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
+            }
           }
-          const uint32_t b16 = bf16_bits(dl);
-          if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
-          // exact in-block corrections: h[k2] += dl * J[i0+k][i0+k2], k2 > k
+          if (lead) stamp(a, t, 9 + 3 * g);
+          uint32_t wcur = g < 2 ? w0 : w1;
+          const int sb = 16 * (g & 1);
+          // fast pass: branch-free decisions from the precomputed log-uniform;
+          // a decision inside the f32 error band is only flagged here
+          const uint32_t wsave = wcur;
+          const float dEsave = dEb;
+          float hsave[16];
 #pragma unroll
-          for (int g = (k + 1) >> 2; g < 16; ++g) {
-            const float4 jv = jb4[k * 16 + g];
-            if (4 * g + 0 > k) h[4 * g + 0] = fmaf(dl, jv.x, h[4 * g + 0]);
-            if (4 * g + 1 > k) h[4 * g + 1] = fmaf(dl, jv.y, h[4 * g + 1]);
-            if (4 * g + 2 > k) h[4 * g + 2] = fmaf(dl, jv.z, h[4 * g + 2]);
-            if (4 * g + 3 > k) h[4 * g + 3] = fmaf(dl, jv.w, h[4 * g + 3]);
+          for (int j = 0; j < 16; ++j) hsave[j] = hs[j];
+          bool unc = false;
+          uint32_t pkg[8];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int k = 16 * g + j;
+            const bool sbit = (wcur >> (sb + j)) & 1u;
+            const float hk = hs[j];
+            const float dn =
+                ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
+            const float lfk = lfb[k * CC + c];
+            const float bd = beta * dn;
+            const float margin = 3e-5f + 1e-6f * fabsf(bd);
+            const bool live = valid && k < kmax;
+            const bool yes = dn >= 0.0f || lfk < bd - margin;
+            const bool no = bd < -24.0f || lfk > bd + margin;
+            unc |= live && !yes && !no;
+            const bool acc = live && yes;
+            const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
+                                          : (sbit ? -1.0f : 1.0f))
+                                 : 0.0f;
+            dl_s[k * CC + c] = dl;
+            const uint32_t b16 = bf16_bits(dl);
+            if (j & 1) pkg[j >> 1] |= b16 << 16; else pkg[j >> 1] = b16;
+            dEb = acc ? dEb - dn : dEb;
+            wcur ^= acc ? (1u << (sb + j)) : 0u;
+            if (j < 15) {  // exact corrections inside the sub-block
+              const float4* jr =
+                  reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
+#pragma unroll
+              for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
+                const float4 v = jr[q4];
+                if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
+                if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
+                if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
+                if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+              }
+            }
           }
+          if (__any_sync(0xffffffffu, unc)) {
+            // rare: redo the sub-block with the exact f64 rule where needed
+            wcur = wsave;
+            dEb = dEsave;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) hs[j] = hsave[j];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int k = 16 * g + j;
+              const bool sbit = (wcur >> (sb + j)) & 1u;
+              const float hk = hs[j];
+              const float dn =
+                  ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
+              const bool acc =
+                  valid && k < kmax &&
+                  metropolis_accept_lf(dn, beta, lfb[k * CC + c], a.seed,
+                                       (uint32_t)inst, sweep, chain_local,
+                                       (uint32_t)(i0 + k));
+              const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
+                                            : (sbit ? -1.0f : 1.0f))
+                                   : 0.0f;
+              dl_s[k * CC + c] = dl;
+              const uint32_t b16 = bf16_bits(dl);
+              if (j & 1) pkg[j >> 1] |= b16 << 16; else pkg[j >> 1] = b16;
+              if (acc) {
+                dEb -= dn;
+                wcur ^= 1u << (sb + j);
+              }
+              if (j < 15) {
+                const float4* jr =
+                    reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
+#pragma unroll
+                for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
+                  const float4 v = jr[q4];
+                  if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
+                  if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
+                  if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
+                  if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+                }
+              }
+            }
+          }
+          if (g < 2) w0 = wcur; else w1 = wcur;
+          // this sub-block's deltas into the A rows (chunks 2g, 2g+1); A is
+          // single-buffered, so the previous block's MMAs must be done
+          if (g == 0 && t > 0) {
+            if (lead) stamp(a, t, 2);
+            a_ok = tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
+            if (lead) stamp(a, t, 3);
+          }
+#pragma unroll
+          for (int qq = 0; qq < F; ++qq) {
+            const int m = qq * CC + c;
+            unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                  ((m >> 3) * 8) * 128 + (m & 7) * 16;
+            if (a_ok) {
+              *reinterpret_cast<uint4*>(rowp + (2 * g) * 128) =
+                  make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+              *reinterpret_cast<uint4*>(rowp + (2 * g + 1) * 128) =
+                  make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
+            }
+          }
+          if (lead) stamp(a, t, 10 + 3 * g);
         }
         if (valid) {
           spins_s[(2 * t) * CC + c] = w0;
           spins_s[(2 * t + 1) * CC + c] = w1;
           dE_s[c] += (double)dEb;
         }
-        if (lead) stamp(a, t, 2);
-        // A is single-buffered: the previous block's MMAs must be done
-        const bool a_free =
-            t == 0 || tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
-        if (lead) stamp(a, t, 3);
-#pragma unroll
-        for (int qq = 0; qq < F && a_free; ++qq) {
-          const int m = qq * CC + c;  // A row = TMEM lane of (slice qq, chain c)
-          unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                ((m >> 3) * 8) * 128 + (m & 7) * 16;
-#pragma unroll
-          for (int kc = 0; kc < 8; ++kc)
-            *reinterpret_cast<uint4*>(rowp + kc * 128) =
-                make_uint4(pk[4 * kc], pk[4 * kc + 1], pk[4 * kc + 2],
-                           pk[4 * kc + 3]);
-        }
         fence_proxy_async();
       }
+      if (lane == 0) stamp(a, t, 20 + warp);
       named_sync_128();
       if (threadIdx.x == 0) {
         stamp(a, t, 4);
         mbar_arrive(sh.a_full);
         mbar_arrive(&sh.jbb_free[t & 1]);
+        mbar_arrive(&sh.lf_free[t & 1]);
       }
     }
     // ----------------------------------------------------------- epilogue
     if (!*sh.abort && NB > 0)
       tc_wait(sh.mma_done, (NB - 1) & 1, sh, status);
     tc::fence_after_sync();
-    if (!*sh.abort) {
+    if (__all_sync(0xffffffffu, !*sh.abort)) {
       for (int j0 = 0; j0 < S; j0 += 32) {
         float v[32];
         tc::tmem_ld32(taddr + lane_base + j0, v);
@@ -453,7 +562,7 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
         tc::commit(sh.mma_done);
       }
     }
-  } else {
+  } else if (warp == 5) {
     // ========================================================= producer
     if (lane == 0) {
       const uint16_t* B = a.tc_b + item.b_off;
@@ -529,6 +638,33 @@ __global__ void __launch_bounds__(192, 1) k_sweep_tc(const TcArgs a) {
     }
   }
 
+  if (warp >= 6) {
+    // ======================================== log-uniforms of the next block
+    const int hid = threadIdx.x - 192;
+    for (int t = 0; t < NB; ++t) {
+      bool go = !*sh.abort;
+      if (go && t >= 2)
+        go = tc_wait(&sh.lf_free[t & 1], ((t >> 1) - 1) & 1, sh, status);
+      if (go) {
+        float* out = lf_s + (t & 1) * 64 * CC;
+        for (int it = hid; it < CC * 16; it += 64) {
+          const int c2 = it % CC, quad = it / CC;
+          const uint32_t cl =
+              (uint32_t)(item.chain0 + c2 - chain_base);
+          uint32_t x[4];
+          draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, cl,
+                (uint32_t)(16 * t + quad), x);
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            out[(4 * quad + e) * CC + c2] = log_uniform_f32(x[e]);
+        }
+      }
+      named_sync_helpers();
+      if (hid == 0) mbar_arrive(&sh.lf_full[t & 1]);
+    }
+  }
+
+  __syncwarp();  // single-lane roles (MMA, producer) rejoin their warps
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
@@ -626,7 +762,7 @@ static cudaError_t launch_tc_t(const TcArgs& a, int count, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
-  k_sweep_tc<F><<<count, 192, TcCfg<F>::BYTES, st>>>(a);
+  k_sweep_tc<F><<<count, 256, TcCfg<F>::BYTES, st>>>(a);
   return cudaGetLastError();
 }
 
