@@ -306,3 +306,65 @@ class PTBatch:
                                         _ptr(out), self._stream.cuda_stream),
               "energy64")
         return out.cpu().numpy()
+
+
+# ---------------------------------------------------------------- AIS
+def run_ais(problem_type: str, J: np.ndarray, h: np.ndarray,
+            temps: np.ndarray, init_states: np.ndarray, *, seed: int,
+            update: str = "sequential", reference: str = "uniform",
+            p: float = 0.5, order: str = "reference"):
+    """Annealed importance sampling on the GPU (pysa/simulation.py:293-317).
+
+    J, h already scaled by the target beta; init_states [Ns, n] (+-1 or
+    0/1).  Returns (samples [Ns, n] float32, log weights [Ns] float64).
+    """
+    ns, n = init_states.shape
+    temps = np.asarray(temps, np.float32)
+    batch = PTBatch(problem_type, [Instance(np.asarray(J, np.float32),
+                                            np.asarray(h, np.float32),
+                                            np.ones(1, np.float32), ns)],
+                    perm_slots=max(len(temps), 1), kernel="plain")
+    batch.set_states(pack_spins(init_states.reshape(ns, 1, n), problem_type,
+                                batch.words), None)
+    temps_d = torch.from_numpy(temps).to(batch.device)
+    log_w = torch.zeros(max(ns, 1), dtype=torch.float64, device=batch.device)
+    opts = _lib.AisOptions(int(seed) & ((1 << 64) - 1),
+                           _lib.RANDOM if update == "random" else
+                           _lib.SEQUENTIAL,
+                           0 if reference == "uniform" else 1,
+                           0 if order == "reference" else 1, len(temps),
+                           float(p))
+    check(batch.lib.pysa_gb_ais(ref(batch.p), ref(batch.s), ref(batch.ws),
+                                ref(opts), temps_d.data_ptr(),
+                                log_w.data_ptr(), batch._stream.cuda_stream),
+          "ais")
+    torch.cuda.synchronize(batch.device)
+    batch.check_status()
+    samples = unpack_spins(batch.spins.cpu().numpy().view("<u4")[:ns], n,
+                           problem_type, np.float32)
+    return samples, log_w.cpu().numpy()[:ns]
+
+
+def logz_exact(problem_type: str, instances: list, beta: float = 1.0):
+    """log sum_s exp(-beta E(s)) of each (J, h) by enumeration on the GPU
+    in f64 (n <= 34)."""
+    lib = _lib.load()
+    insts = [Instance(np.asarray(J, np.float32), np.asarray(h, np.float32),
+                      np.ones(1, np.float32), 0) for J, h in instances]
+    batch = PTBatch(problem_type, insts, kernel="plain")
+    parts = int(lib.pysa_gb_logz_parts(len(insts), batch.max_n))
+    if parts < 0:
+        raise ValueError("exact log Z supports 1 <= n <= 34")
+    pm = torch.empty(parts, dtype=torch.float64, device=batch.device)
+    ps = torch.empty(parts, dtype=torch.float64, device=batch.device)
+    check(lib.pysa_gb_logz_exact(ref(batch.p), float(beta), pm.data_ptr(),
+                                 ps.data_ptr(), batch._stream.cuda_stream),
+          "logz")
+    m = pm.cpu().numpy().reshape(len(insts), -1)
+    sm = ps.cpu().numpy().reshape(len(insts), -1)
+    out = []
+    for mi, si in zip(m, sm):
+        ok = np.isfinite(mi)
+        top = mi[ok].max()
+        out.append(float(top + np.log(np.sum(si[ok] * np.exp(mi[ok] - top)))))
+    return np.array(out)

@@ -14,7 +14,9 @@ Differences from the reference, all deliberate:
   * All reads run concurrently; 'runtime (us)' and 'init_time (us)' are the
     batch times divided by num_reads.
   * Sweeps compute in float32 whatever float_type is; float_type sets the
-    output dtypes (pysa/sa.py:204-205 casts the problem the same way).
+    output dtypes (pysa/sa.py:204-205 casts the problem the same way).  With
+    float_type='float64' the returned energies and best energies are the
+    exact (f64) energies of the returned states.
   * num_sweeps < 1 raises ValueError (the reference fails with
     UnboundLocalError at pysa/simulation.py:181).
 """
@@ -28,7 +30,7 @@ from typing import Any, List
 import numpy as np
 
 from . import ais as _ais
-from .engine import Instance, PTBatch, pack_spins, unpack_spins
+from .engine import Instance, PTBatch, pack_spins, run_ais, unpack_spins
 
 Vector = List[float]
 
@@ -333,6 +335,14 @@ class Solver(object):
                         np.dtype(self.float_type).type(be[r, k]))
                     best_sweeps.append(int(bs[r, k]))
 
+        if not recompute_energy and np.dtype(self.float_type) == np.float64:
+            # the sweeps ran in float32; a float64 run reports the exact
+            # energies of its states, as the reference's float64 sweeps do
+            allst = np.concatenate([out_states_all.reshape(-1, N),
+                                    np.stack(best_states)]) if Rd else None
+            e64 = self._energies64(allst) if Rd else np.zeros(0)
+            energies = e64[:Rd * R].reshape(Rd, R)
+            best_energies = [np.float64(x) for x in e64[Rd * R:]]
         if recompute_energy:  # pysa/sa.py:372-377 (original dtype)
             dt = self.couplings.dtype
             allst = np.concatenate([out_states_all.reshape(-1, N),
@@ -392,18 +402,16 @@ class Solver(object):
         pysa/simulation.py:305-316 does; 'standard' weights before the sweep
         (the unbiased AIS ordering).
         """
-        from . import _lib
-        from ._lib import check
         if reference_prob == "uniform":
             logZ0 = _ais.uniform_partition_fun(self.n_vars)
-            ref_code, p = 0, 0.5
+            p = 0.5
 
             def init():
                 return _ais.uniform_prob_initialization(
                     self.n_vars, self.problem_type, None)
         elif reference_prob == "bernoulli":
             logZ0 = _ais.bernoulli_partition_fun(self.n_vars)
-            ref_code, p = 1, float(reference_args[0])
+            p = float(reference_args[0])
 
             def init():
                 return _ais.bernoulli_prob_initialization(
@@ -423,32 +431,11 @@ class Solver(object):
                             for _ in range(num_samps)])
         if seed is None:
             seed = secrets.randbits(64)
-        import torch
-        batch = PTBatch(self.problem_type, [
-            Instance(np.asarray(couplings, np.float32),
-                     np.asarray(local_fields, np.float32),
-                     np.ones(1, np.float32), int(num_samps))
-        ], perm_slots=max(int(num_temps), 1))
-        batch.set_states(pack_spins(initial.reshape(num_samps, 1, -1),
-                                    self.problem_type, batch.words), None)
-        temps_d = torch.from_numpy(temps.astype(np.float32)).to(batch.device)
-        log_w = torch.zeros(max(num_samps, 1), dtype=torch.float64,
-                            device=batch.device)
-        opts = _lib.AisOptions(int(seed) & ((1 << 64) - 1),
-                               _lib.RANDOM if update_strategy == 'random' else
-                               _lib.SEQUENTIAL, ref_code,
-                               0 if ais_order == 'reference' else 1,
-                               int(num_temps), p)
-        check(batch.lib.pysa_gb_ais(_lib.ref(batch.p), _lib.ref(batch.s),
-                                    _lib.ref(batch.ws), _lib.ref(opts),
-                                    temps_d.data_ptr(), log_w.data_ptr(),
-                                    batch._stream.cuda_stream), "ais")
-        torch.cuda.synchronize()
-        batch.check_status()
-        log_omegas = log_w.cpu().numpy()[:num_samps]
-        samples = unpack_spins(
-            batch.spins.cpu().numpy().view("<u4")[:num_samps], self.n_vars,
-            self.problem_type, self.float_type)
+        samples, log_omegas = run_ais(
+            self.problem_type, couplings, local_fields, temps, initial,
+            seed=int(seed), update=update_strategy, reference=reference_prob,
+            p=p, order=ais_order)
+        samples = samples.astype(self.float_type)
         logZf = _ais.omegas_to_partition(np.array(log_omegas), logZ0)
         lomax = log_omegas.max()
         normalization = np.sum(np.exp(log_omegas - lomax))

@@ -1,0 +1,144 @@
+"""Solver drop-in on the GPU against the reference's own frames and tests.
+
+* Frames recorded from pysa.sa.Solver on problems whose outcome does not
+  depend on the sweep random stream (J = h = 0): initial-state draws from the
+  global NumPy RNG, the ladder, the temps column (inverse-permutation order
+  when unsorted), best tracking of both drivers and log_Zf must all match.
+* The invariants of the reference's tests (tests/tests_ising_sequential.py):
+  best_energy equals the energy of best_state and is never below the
+  brute-force minimum.
+* The planted Wishart N=50 instance shipped with the reference tutorials
+  reaches its known ground energy.
+"""
+import ast
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+FRAMES = ["solver_ising_par", "solver_ising_seq_sorted", "solver_qubo_logz",
+          "solver_qubo_ones", "solver_ising_r1", "solver_ising_r2_nopt"]
+
+
+@pytest.mark.parametrize("name", FRAMES)
+def test_solver_frames_match_reference(name):
+    from pysa_gb300 import Solver
+    g = golden(name)
+    n = int(g["n"])
+    kw = ast.literal_eval(str(g["kwargs"]))
+    np.random.seed(int(g["np_seed"]))
+    rows = Solver(np.zeros((n, n)), str(g["problem_type"]),
+                  "float32").metropolis_update(return_dataframe=False,
+                                               seed=1, **kw)
+    assert list(rows[0].keys()) == [str(c) for c in g["columns"]]
+    for key in ("states", "energies", "best_state", "temps"):
+        got = np.stack([np.asarray(r[key]) for r in rows])
+        assert got.dtype == g[key].dtype, key
+        assert np.array_equal(got, g[key]), key
+    assert np.array_equal([r["best_energy"] for r in rows], g["best_energy"])
+    assert np.array_equal([r["min_sweeps"] for r in rows], g["min_sweeps"])
+    assert np.array_equal([r["num_sweeps"] for r in rows], g["num_sweeps"])
+    if "log_Zf" in g:
+        np.testing.assert_allclose([r["log_Zf"] for r in rows], g["log_Zf"],
+                                   rtol=1e-12)
+
+
+def _gen_random_problem(rng, n):
+    c = 2 * rng.random((n, n)) - 1
+    return (c + c.T) / 2
+
+
+def _brute_min(P, ptype):
+    n = len(P)
+    h = np.diag(P).copy()
+    J = P.copy()
+    np.fill_diagonal(J, 0)
+    lo = -1.0 if ptype == "ising" else 0.0
+    idx = np.arange(2**n)
+    S = np.where((idx[:, None] >> np.arange(n)) & 1, 1.0, lo)
+    E = np.einsum("si,ij,sj->s", S, J, S) / 2 + S @ h
+    return E.min()
+
+
+@pytest.mark.parametrize("ptype,beta", [("ising", 1.0), ("qubo", 10.0)])
+@pytest.mark.parametrize("parallel", [True, False])
+@pytest.mark.parametrize("update", ["sequential", "random"])
+def test_best_energy_consistent_and_above_brute_force(ptype, beta, parallel,
+                                                      update):
+    from pysa_gb300 import Solver
+    rng = np.random.default_rng(12)
+    for n in (12, 16):
+        P = _gen_random_problem(rng, n)
+        s = Solver(P, ptype, "float64")
+        rows = s.metropolis_update(num_sweeps=2000, num_reads=2,
+                                   temps=[1.0 / beta], update_strategy=update,
+                                   parallel=parallel, return_dataframe=False,
+                                   seed=n)
+        emin = _brute_min(P, ptype)
+        for r in rows:
+            assert np.isclose(r["best_energy"], s.get_energy(r["best_state"]))
+            assert np.round(r["best_energy"], 5) >= np.round(emin, 5)
+            for st, e in zip(r["states"], r["energies"]):
+                assert np.isclose(e, s.get_energy(st), atol=1e-5)
+
+
+def test_update_at_infinite_temperature_flips_every_spin():
+    """pysa tests: at beta = 0 every attempt is accepted."""
+    from pysa_gb300 import Solver
+    rng = np.random.default_rng(3)
+    P = _gen_random_problem(rng, 64)
+    s = Solver(P, "ising", "float32")
+    x0 = (2 * rng.integers(0, 2, (3, 64)) - 1).astype(np.float32)
+    rows = s.metropolis_update(num_sweeps=1, num_reads=1, temps=[np.inf] * 3,
+                               initialize_strategy=x0, use_pt=False,
+                               update_strategy="sequential",
+                               return_dataframe=False, seed=2)
+    assert np.array_equal(rows[0]["states"], -x0)
+    for st, e in zip(rows[0]["states"], rows[0]["energies"]):
+        assert np.isclose(e, s.get_energy(st, dtype="float32"), rtol=1e-5,
+                          atol=1e-4)
+
+
+def test_planted_wishart_ground_energy():
+    """Wishart N=50 fixture of the reference tutorials: 2 * E_best equals the
+    recorded ground energy."""
+    from pysa_gb300 import Solver
+    g = golden("wishart50")
+    s = Solver(g["problem"], "ising", "float32")
+    np.random.seed(0)
+    rows = s.metropolis_update(num_sweeps=3000, num_reads=16, num_replicas=32,
+                               min_temp=3e3, max_temp=3e5,
+                               update_strategy="sequential",
+                               return_dataframe=False, seed=11)
+    best = min(float(r["best_energy"]) for r in rows)
+    assert 2 * best == float(g["ground_energy_x2"])
+
+
+def test_pt_exchange_only_permutes():
+    """pysa tests test_pt: the exchange permutes temperatures only; energies
+    stay consistent with the states."""
+    from pysa_gb300 import Solver
+    rng = np.random.default_rng(9)
+    P = _gen_random_problem(rng, 40)
+    s = Solver(P, "ising", "float32")
+    rows = s.metropolis_update(num_sweeps=30, num_reads=3, num_replicas=6,
+                               min_temp=0.3, max_temp=3.0,
+                               return_dataframe=False, seed=5)
+    ladder = sorted(1 / np.asarray(rows[0]["temps"]))
+    for r in rows:
+        assert np.allclose(sorted(1 / np.asarray(r["temps"])), ladder)
+        for st, e in zip(r["states"], r["energies"]):
+            assert np.isclose(e, s.get_energy(st, dtype="float32"), rtol=1e-5,
+                              atol=1e-4)
+
+
+def test_background_returns_future():
+    from pysa_gb300 import Solver
+    s = Solver(np.eye(8), "qubo")
+    fut = s.metropolis_update(num_sweeps=4, num_reads=2, send_background=True,
+                              return_dataframe=False, seed=1)
+    rows = fut.result(timeout=120)
+    assert len(rows) == 2 and rows[0]["num_sweeps"] == 4
