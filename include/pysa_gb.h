@@ -210,6 +210,26 @@ int pysa_gb_sweeps(const pysa_gb_problems *p, pysa_gb_state *s,
                    pysa_gb_workspace *ws, const pysa_gb_options *o,
                    int32_t num_sweeps, void *stream);
 
+/* Allocation-free form of pysa_gb_prepare + pysa_gb_sweeps on the plain
+ * CUDA-core kernel.  No counterpart in the reference: it exists for callers
+ * that cannot allocate device memory themselves (a plugin inside a host
+ * application whose device memory is owned by the host's pool, a loop that
+ * cannot afford cudaMalloc's implicit synchronisation, C code without a
+ * device allocator).  The caller passes only inputs and outputs; the local
+ * fields, visiting orders, packed couplings and work list live in one
+ * library-owned device array of 64 MiB, held on every GPU that loads the
+ * library until the process exits.  Batches needing more scratch are
+ * rejected with PYSA_GB_ERR_SIZE.  `init` = 1 computes energies from the
+ * spins and resets best_*; 0 continues from the caller's energies and best_*.
+ * Fields are rebuilt from the spins on every call.  All calls share the
+ * array: calls that overlap on the GPU race.  The first call on each device
+ * resolves the array's address and should come before any stream capture.
+ * Sequential and random order; never the tensor-core kernel. */
+int pysa_gb_sweeps_noalloc(const pysa_gb_problems *p, pysa_gb_state *s,
+                           const pysa_gb_host_tables *host,
+                           const pysa_gb_options *o, int32_t init,
+                           int32_t num_sweeps, void *stream);
+
 /* Energies in f64 of `count` bit-packed states of instance `inst`
  * (get_energy, pysa/ising.py:32-37) with f64 couplings J64 (n x ld64). */
 int pysa_gb_energy64(int32_t problem_type, int32_t n, int32_t ld64,

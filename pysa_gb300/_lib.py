@@ -89,6 +89,7 @@ def load() -> ctypes.CDLL:
         "pysa_gb_tc_setup": ([P, P, P, P], ctypes.c_int),
         "pysa_gb_prepare": ([P, P, P, I32, I32, I32, P], ctypes.c_int),
         "pysa_gb_sweeps": ([P, P, P, P, I32, P], ctypes.c_int),
+        "pysa_gb_sweeps_noalloc": ([P, P, P, P, I32, I32, P], ctypes.c_int),
         "pysa_gb_energy64": ([I32, I32, I32, P, P, P, I32, I64, P, P],
                              ctypes.c_int),
         "pysa_gb_unpack": ([I32, I32, P, I32, I64, P, I32, P], ctypes.c_int),

@@ -35,12 +35,28 @@ static int row_floats(int v) {
 
 static int lane_stride(int v) { return row_floats(v) / 32; }
 
+PlainItemPlan make_item_plan() {
+  PlainItemPlan plan;
+  for (int v = 0; v < kNumPlainVariants; ++v) {
+    const PlainVariant& pv = plain_variant(v);
+    plan.nc[v] = pv.nc;
+    plan.cpb[v] = pv.gw * pv.w;
+    plan.row_floats[v] = row_floats(v);
+    plan.start[v] = 0;
+  }
+  return plan;
+}
+
 static thread_local std::string g_last_error;
 static unsigned long long* g_tc_trace = nullptr;  // diagnostics, see below
 
 static int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
+}
+
+int pysa_gb_internal_fail(int code, const char* msg) {
+  return fail(code, msg);
 }
 
 static int cuda_fail(cudaError_t e, const char* where) {
