@@ -271,6 +271,88 @@ int64_t pysa_gb_logz_parts(int32_t num_instances, int32_t max_n);
 int pysa_gb_logz_exact(const pysa_gb_problems *p, double beta,
                        double *part_max, double *part_sum, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Learned flip proposal.  No counterpart in the reference: these entry
+ * points add a Metropolis-Hastings move for the coldest replica of every
+ * read, proposed by a per-instance MLP  nn -> hidden -> nn  (ReLU hidden
+ * layer, one Bernoulli flip logit per spin) that is trained online on pairs
+ * of cold states.  Weights are FP32 masters with BF16 copies for the tensor
+ * cores; GEMMs accumulate in FP32.  Every array is device memory, stacked
+ * over instances with the sizes given beside it (I = num_instances,
+ * B = batch, H = hidden).  nn % 256 == 0, hidden % 256 == 0,
+ * batch % 128 == 0, nn >= max_n of the problems.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t num_instances, n, hidden, batch;
+  float *w1, *b1, *w2, *b2;          /* [I][H][nn], [I][H], [I][nn][H], [I][nn] */
+  float *m1, *v1, *mb1, *vb1;        /* Adam moments of w1, b1 */
+  float *m2, *v2, *mb2, *vb2;        /* Adam moments of w2, b2 */
+  float *dw1, *db1, *dw2, *db2;      /* gradients, shapes of w1, b1, w2, b2 */
+  uint16_t *w1_p, *w2_p, *w2t_p;     /* BF16 tiles of w1, w2, w2^T [I][H*nn] */
+  float *x, *a1, *z2, *dz2, *da1;    /* [I][B][nn], [I][B][H], [I][B][nn] x2,
+                                        [I][B][H] */
+  uint16_t *pa, *pb;                 /* operand tiles [I][B*max(nn,H)] each */
+  float *loss;                       /* [I] mean BCE of the last backward */
+  int32_t *status;                   /* bounded-wait status word */
+} pysa_gb_mlp;
+
+/* Per-proposal scratch: flip masks, delta = s' - s and J delta [I][B][nn];
+ * log q forward / reverse and accepted dE [I][B]. */
+typedef struct {
+  float *flip, *delta, *jd;
+  float *logq_fwd, *logq_rev, *de;
+} pysa_gb_proposal_scratch;
+
+/* BF16 copies of w1, w2 and w2^T after the masters changed. */
+int pysa_gb_mlp_sync_weights(const pysa_gb_mlp *m, void *stream);
+/* z2 = W2 relu(W1 x + b1) + b2 for the B rows of x of every instance. */
+int pysa_gb_mlp_forward(const pysa_gb_mlp *m, void *stream);
+/* Gradients of the row-weighted mean (weights [I][B]) of the per-row sum of
+ * binary cross-entropies between sigmoid(z2) and target [I][B][nn]; uses
+ * the activations of the last forward.  loss[i] = that mean. */
+int pysa_gb_mlp_backward(const pysa_gb_mlp *m, const float *target,
+                         const float *row_weight, void *stream);
+/* One Adam step (Kingma & Ba 2015) on every parameter; step >= 1 is the
+ * bias-correction count.  Refreshes the BF16 copies. */
+int pysa_gb_mlp_adam(const pysa_gb_mlp *m, float lr, float beta1, float beta2,
+                     float eps, int32_t step, void *stream);
+/* Training pairs from two snapshots [I][B][words]: x = snapshot a as spin
+ * values, target = (a != b) per spin. */
+int pysa_gb_mlp_pairs(const pysa_gb_mlp *m, int32_t problem_type,
+                      const int32_t *n_inst, const uint32_t *snap_a,
+                      const uint32_t *snap_b, int32_t words, float *target,
+                      void *stream);
+/* rows[i][r] = chain holding the largest beta of read r of instance i
+ * (first on ties), -1 for r >= reads[i] or when enabled[i] == 0 (enabled
+ * may be NULL: all instances). */
+int pysa_gb_cold_rows(const pysa_gb_problems *p, const pysa_gb_state *s,
+                      const int32_t *enabled, int32_t batch, int32_t *rows,
+                      void *stream);
+/* out[i][r][:] = spins of chain rows[i][r] (zeros for -1). */
+int pysa_gb_snapshot(const pysa_gb_problems *p, const pysa_gb_state *s,
+                     const int32_t *rows, int32_t batch, uint32_t *out,
+                     void *stream);
+/* BF16 copies of the couplings as the B operand of J delta:
+ * out[i][t] (t < terms) = tile(J_field^T), J_field[j][k] = change of field j
+ * per unit change of spin k; terms = 2 adds the residual J - bf16(J). */
+int64_t pysa_gb_proposal_j_elems(int32_t num_instances, int32_t nn,
+                                 int32_t terms);
+int pysa_gb_pack_proposal_j(const pysa_gb_problems *p,
+                            const pysa_gb_host_tables *host, int32_t nn,
+                            int32_t terms, uint16_t *out, void *stream);
+/* One proposal for every row: s' from the flip mask sampled from
+ * sigmoid(z2(s)) with uniforms of stream (PROPOSAL, inst, round, chain, j);
+ * accept iff log u < -beta dE + log q(s|s') - log q(s'|s) (u from index
+ * 0xFFFFFFFF of the same stream), dE = delta.(H + J delta / 2) in f32.
+ * Accepted rows get new spins, fields, energies and best_* (best_sweep =
+ * sweep_counter - 1).  accepted[i] += accepted rows of instance i. */
+int pysa_gb_propose(const pysa_gb_problems *p, pysa_gb_state *s,
+                    pysa_gb_workspace *ws, const pysa_gb_mlp *m,
+                    const int32_t *rows, const uint16_t *j_packed,
+                    int32_t terms, const pysa_gb_proposal_scratch *sc,
+                    uint64_t seed, uint32_t round, int32_t *accepted,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,7 @@ ERR_TIMEOUT = -4
 
 P = ctypes.c_void_p
 I32, I64, U64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64
+F32 = ctypes.c_float
 
 
 class Problems(ctypes.Structure):
@@ -58,6 +59,20 @@ class Options(ctypes.Structure):
                 ("phases", I32), ("recompute_every", I32)]
 
 
+class Mlp(ctypes.Structure):
+    _fields_ = [("num_instances", I32), ("n", I32), ("hidden", I32),
+                ("batch", I32)] + [(k, P) for k in (
+                    "w1", "b1", "w2", "b2", "m1", "v1", "mb1", "vb1", "m2",
+                    "v2", "mb2", "vb2", "dw1", "db1", "dw2", "db2", "w1_p",
+                    "w2_p", "w2t_p", "x", "a1", "z2", "dz2", "da1", "pa", "pb",
+                    "loss", "status")]
+
+
+class ProposalScratch(ctypes.Structure):
+    _fields_ = [(k, P) for k in ("flip", "delta", "jd", "logq_fwd",
+                                 "logq_rev", "de")]
+
+
 class AisOptions(ctypes.Structure):
     _fields_ = [("seed", U64), ("update", I32), ("reference", I32),
                 ("order", I32), ("num_temps", I32), ("p", ctypes.c_double)]
@@ -96,6 +111,17 @@ def load() -> ctypes.CDLL:
         "pysa_gb_ais": ([P, P, P, P, P, P, P], ctypes.c_int),
         "pysa_gb_logz_parts": ([I32, I32], I64),
         "pysa_gb_logz_exact": ([P, ctypes.c_double, P, P, P], ctypes.c_int),
+        "pysa_gb_mlp_sync_weights": ([P, P], ctypes.c_int),
+        "pysa_gb_mlp_forward": ([P, P], ctypes.c_int),
+        "pysa_gb_mlp_backward": ([P, P, P, P], ctypes.c_int),
+        "pysa_gb_mlp_adam": ([P, F32, F32, F32, F32, I32, P], ctypes.c_int),
+        "pysa_gb_mlp_pairs": ([P, I32, P, P, P, I32, P, P], ctypes.c_int),
+        "pysa_gb_cold_rows": ([P, P, P, I32, P, P], ctypes.c_int),
+        "pysa_gb_snapshot": ([P, P, P, I32, P, P], ctypes.c_int),
+        "pysa_gb_proposal_j_elems": ([I32, I32, I32], I64),
+        "pysa_gb_pack_proposal_j": ([P, P, I32, I32, P, P], ctypes.c_int),
+        "pysa_gb_propose": ([P, P, P, P, P, P, I32, P, U64, ctypes.c_uint32,
+                             P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
