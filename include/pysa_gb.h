@@ -341,7 +341,9 @@ int pysa_gb_pack_proposal_j(const pysa_gb_problems *p,
                             const pysa_gb_host_tables *host, int32_t nn,
                             int32_t terms, uint16_t *out, void *stream);
 /* One proposal for every row: s' from the flip mask sampled from
- * sigmoid(z2(s)) with uniforms of stream (PROPOSAL, inst, round, chain, j);
+ * sigmoid(z2(s) + c(s)) with uniforms of stream (PROPOSAL, inst, round,
+ * chain, j); c(s) = 0 when target_flips <= 0, else the shift that makes the
+ * expected number of flips target_flips (same rule for the reverse pass);
  * accept iff log u < -beta dE + log q(s|s') - log q(s'|s) (u from index
  * 0xFFFFFFFF of the same stream), dE = delta.(H + J delta / 2) in f32.
  * Accepted rows get new spins, fields, energies and best_* (best_sweep =
@@ -350,8 +352,8 @@ int pysa_gb_propose(const pysa_gb_problems *p, pysa_gb_state *s,
                     pysa_gb_workspace *ws, const pysa_gb_mlp *m,
                     const int32_t *rows, const uint16_t *j_packed,
                     int32_t terms, const pysa_gb_proposal_scratch *sc,
-                    uint64_t seed, uint32_t round, int32_t *accepted,
-                    void *stream);
+                    uint64_t seed, uint32_t round, float target_flips,
+                    int32_t *accepted, void *stream);
 
 #ifdef __cplusplus
 }

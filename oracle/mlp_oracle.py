@@ -79,6 +79,22 @@ def adam(w, m, v, g, lr, beta1, beta2, eps, step):
     return w - lr * (m / c1) / (np.sqrt(v / c2) + eps), m, v
 
 
+def flip_shift(z, k):
+    """Shift c with sum_j sigmoid(z_j + c) = k (40 bisection steps on
+    [-60, 60], as the GPU does); 0 when k <= 0."""
+    if k <= 0:
+        return 0.0
+    lo, hi = -60.0, 60.0
+    z = np.asarray(z, np.float64)
+    for _ in range(40):
+        c = 0.5 * (lo + hi)
+        if sigmoid(z + c).sum() > k:
+            hi = c
+        else:
+            lo = c
+    return 0.5 * (lo + hi)
+
+
 def flip_mask(z, u):
     """f_j = u_j < sigmoid(z_j) and log q(f | z)."""
     p = sigmoid(np.asarray(z, np.float64))

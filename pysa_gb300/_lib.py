@@ -121,7 +121,7 @@ def load() -> ctypes.CDLL:
         "pysa_gb_proposal_j_elems": ([I32, I32, I32], I64),
         "pysa_gb_pack_proposal_j": ([P, P, I32, I32, P, P], ctypes.c_int),
         "pysa_gb_propose": ([P, P, P, P, P, P, I32, P, U64, ctypes.c_uint32,
-                             P, P], ctypes.c_int),
+                             F32, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -130,14 +130,34 @@ __device__ __forceinline__ float log_sigmoid(float z) {
   return -(fmaxf(-z, 0.0f) + log1pf(expf(-fabsf(z))));
 }
 
-// Warp per row: sample the flip mask from sigmoid(z), log q(s'|s), and the
-// proposed state x' (written over x) with delta = x' - x.  Flip j iff
-// u < sigmoid(z_j), u = f32 of the uniform of stream (PROPOSAL, inst, round,
-// chain, j).
+// Proposal-size control: the shift c with sum_{j<n} sigmoid(z_j + c) = k,
+// by 40 bisection steps on [-60, 60] (c saturates at the ends when k is out
+// of reach).  Warp-collective and a deterministic function of z, so the
+// forward and the reverse pass use the same rule.  k <= 0: no shift.
+__device__ float flip_shift(const float* z, int n, float k, int lane) {
+  if (k <= 0.0f) return 0.0f;
+  float lo = -60.0f, hi = 60.0f;
+  for (int it = 0; it < 40; ++it) {
+    const float c = 0.5f * (lo + hi);
+    float sum = 0.0f;
+    for (int j = lane; j < n; j += 32) sum += 1.0f / (1.0f + expf(-(z[j] + c)));
+    sum = warp_sum(sum);
+    if (sum > k)
+      hi = c;
+    else
+      lo = c;
+  }
+  return 0.5f * (lo + hi);
+}
+
+// Warp per row: sample the flip mask from sigmoid(z + c) (c from
+// flip_shift), log q(s'|s), and the proposed state x' (written over x) with
+// delta = x' - x.  Flip j iff u < sigmoid(z_j + c), u = f32 of the uniform
+// of stream (PROPOSAL, inst, round, chain, j).
 __global__ void k_sample_flips(const pysa_gb_problems p, const int32_t* rows,
                                int B, int nn, const float* z, float* x,
                                float* flip, float* delta, float* logq,
-                               uint64_t seed, uint32_t round) {
+                               uint64_t seed, uint32_t round, float k_flips) {
   const int i = blockIdx.y;
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -146,11 +166,12 @@ __global__ void k_sample_flips(const pysa_gb_problems p, const int32_t* rows,
   const int n_i = p.n[i];
   const bool ising = p.problem_type == PYSA_GB_ISING;
   const int64_t o = ((int64_t)i * B + r) * nn;
+  const float shift = c >= 0 ? flip_shift(z + o, n_i, k_flips, lane) : 0.0f;
   float lq = 0.0f;
   for (int j = lane; j < nn; j += 32) {
     float f = 0.0f, d = 0.0f;
     if (c >= 0 && j < n_i) {
-      const float zz = z[o + j];
+      const float zz = z[o + j] + shift;
       const float u = (float)uniform64(draw1(seed, TAG_PROPOSAL, (uint32_t)i,
                                              round, (uint32_t)c, (uint32_t)j));
       const float pj = 1.0f / (1.0f + expf(-zz));
@@ -173,7 +194,8 @@ __global__ void k_sample_flips(const pysa_gb_problems p, const int32_t* rows,
 // log q(s|s') of the same mask under the logits at s'.
 __global__ void k_logq_reverse(const int32_t* rows, int B, int nn,
                                const int32_t* n_inst, const float* z,
-                               const float* flip, float* logq) {
+                               const float* flip, float* logq,
+                               float k_flips) {
   const int i = blockIdx.y;
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -182,8 +204,9 @@ __global__ void k_logq_reverse(const int32_t* rows, int B, int nn,
   const int64_t o = ((int64_t)i * B + r) * nn;
   float lq = 0.0f;
   if (rows[(int64_t)i * B + r] >= 0) {
+    const float shift = flip_shift(z + o, n_i, k_flips, lane);
     for (int j = lane; j < n_i; j += 32) {
-      const float zz = z[o + j];
+      const float zz = z[o + j] + shift;
       lq += flip[o + j] > 0.0f ? log_sigmoid(zz) : log_sigmoid(-zz);
     }
   }
@@ -527,8 +550,8 @@ int pysa_gb_propose(const pysa_gb_problems* p, pysa_gb_state* s,
                     pysa_gb_workspace* ws, const pysa_gb_mlp* m,
                     const int32_t* rows, const uint16_t* j_packed,
                     int32_t terms, const pysa_gb_proposal_scratch* sc,
-                    uint64_t seed, uint32_t round, int32_t* accepted,
-                    void* stream) {
+                    uint64_t seed, uint32_t round, float target_flips,
+                    int32_t* accepted, void* stream) {
   if (!p || !s || !ws || !mlp_ok(m) || !rows || !j_packed || !sc ||
       !accepted || terms < 1 || terms > 2)
     return mlp_fail("propose: bad argument");
@@ -543,10 +566,10 @@ int pysa_gb_propose(const pysa_gb_problems* p, pysa_gb_state* s,
   if ((e = mlp_forward(m, st))) return cuda_check(e, "propose forward");
   k_sample_flips<<<dim3((B + 7) / 8, I), 256, 0, st>>>(
       *p, rows, B, n, m->z2, m->x, sc->flip, sc->delta, sc->logq_fwd, seed,
-      round);
+      round, target_flips);
   if ((e = mlp_forward(m, st))) return cuda_check(e, "propose reverse");
   k_logq_reverse<<<dim3((B + 7) / 8, I), 256, 0, st>>>(
-      rows, B, n, p->n, m->z2, sc->flip, sc->logq_rev);
+      rows, B, n, p->n, m->z2, sc->flip, sc->logq_rev, target_flips);
   // jd = delta J_field^T: M = B, N = nn, K = nn; terms accumulate
   if ((e = pack(m, sc->delta, n, (int64_t)B * n, B, n, 0, 128, m->pa, st)))
     return cuda_check(e, "propose J delta");

@@ -56,12 +56,17 @@ class LearnedProposal:
     lr, adam_betas, eps: Adam hyper-parameters.
     init_flips: expected number of flipped spins of the untrained network
         (sets the output bias).
+    target_flips: when > 0, every proposal is rescaled (one logit shift per
+        state, applied the same way in the reverse pass) to flip this many
+        spins on average; the network then decides which spins.
     """
 
     def __init__(self, batch: PTBatch, hidden: int = 1024, lr: float = 1e-3,
                  adam_betas=(0.9, 0.999), eps: float = 1e-8,
-                 init_seed: int = 0, init_flips: float = 2.0):
+                 init_seed: int = 0, init_flips: float = 2.0,
+                 target_flips: float = 0.0):
         self.lib = _lib.load()
+        self.target_flips = float(target_flips)
         self.b = batch
         dev = batch.device
         I = len(batch.instances)
@@ -98,6 +103,7 @@ class LearnedProposal:
         self.sc = _lib.ProposalScratch(*(_ptr(self.sc_t[k]) for k in (
             "flip", "delta", "jd", "logq_fwd", "logq_rev", "de")))
         self.rows = z(I, B, dt=torch.int32)
+        self.obs_rows = z(I, B, dt=torch.int32)
         self.enabled = torch.ones(I, dtype=torch.int32, device=dev)
         self.accepted = z(I, dt=torch.int32)
         self.snap = [z(I, B, self.words, dt=torch.int32) for _ in range(2)]
@@ -189,26 +195,31 @@ class LearnedProposal:
 
     # --------------------------------------------------------- online loop
     def observe(self) -> bool:
-        """Snapshot the cold state of every read; with a previous snapshot,
-        train one step on the pair (previous -> current).  Returns whether
-        a training step ran."""
+        """Training data from the chains themselves: with a previous
+        observation, snapshot the same chains again (the pair is their state
+        then and now, target = the spins that changed) and train one step on
+        it; then record the chains now holding the coldest slot for the next
+        pair.  Returns whether a training step ran."""
         b = self.b
         st = self._st()
-        check(self.lib.pysa_gb_cold_rows(ref(b.p), ref(b.s), 0, self.B,
-                                         _ptr(self.rows), st), "cold rows")
-        cur, prev = self.snap[1], self.snap[0]
-        check(self.lib.pysa_gb_snapshot(ref(b.p), ref(b.s), _ptr(self.rows),
-                                        self.B, _ptr(cur), st), "snapshot")
         trained = False
         if self.have_snap:
+            check(self.lib.pysa_gb_snapshot(ref(b.p), ref(b.s),
+                                            _ptr(self.obs_rows), self.B,
+                                            _ptr(self.snap[1]), st), "snapshot")
             check(self.lib.pysa_gb_mlp_pairs(
-                ref(self.m), b.ptype, _ptr(self.n_inst), _ptr(prev),
-                _ptr(cur), self.words, _ptr(self.target), st), "pairs")
+                ref(self.m), b.ptype, _ptr(self.n_inst), _ptr(self.snap[0]),
+                _ptr(self.snap[1]), self.words, _ptr(self.target), st),
+                "pairs")
             self.forward()
             self.train_step()
             self.stats.train_steps += 1
             trained = True
-        self.snap = [cur, prev]
+        check(self.lib.pysa_gb_cold_rows(ref(b.p), ref(b.s), 0, self.B,
+                                         _ptr(self.obs_rows), st), "cold rows")
+        check(self.lib.pysa_gb_snapshot(ref(b.p), ref(b.s),
+                                        _ptr(self.obs_rows), self.B,
+                                        _ptr(self.snap[0]), st), "snapshot")
         self.have_snap = True
         return trained
 
@@ -223,8 +234,8 @@ class LearnedProposal:
         check(self.lib.pysa_gb_propose(
             ref(b.p), ref(b.s), ref(b.ws), ref(self.m), _ptr(self.rows),
             _ptr(self.j_packed), self.terms, ref(self.sc),
-            seed & ((1 << 64) - 1), round_ & 0xFFFFFFFF, _ptr(self.accepted),
-            st), "propose")
+            seed & ((1 << 64) - 1), round_ & 0xFFFFFFFF, self.target_flips,
+            _ptr(self.accepted), st), "propose")
 
 
 def run_with_proposals(batch: PTBatch, prop: LearnedProposal | None,

@@ -9,16 +9,11 @@ a BF16 rounding boundary moves downstream results by one BF16 ulp (2^-8
 relative) of that value, hence the 2e-3-of-scale bounds on logits and
 gradients.
 """
-import os
-import sys
-
 import numpy as np
 import pytest
 import torch
 
-from conftest import ROOT
-
-from oracle import mlp_oracle as mo  # noqa: E402
+from oracle import mlp_oracle as mo
 
 pytestmark = pytest.mark.gpu
 
@@ -125,7 +120,8 @@ def test_training_fits_a_learnable_target():
     assert losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
 
 
-def test_flip_sampling_and_log_q_match_oracle(oracle):
+@pytest.mark.parametrize("target_flips", [0.0, 4.0])
+def test_flip_sampling_and_log_q_match_oracle(oracle, target_flips):
     from pysa_gb300.proposal import LearnedProposal
     from pysa_gb300 import unpack_spins
     rng = np.random.default_rng(2)
@@ -133,7 +129,8 @@ def test_flip_sampling_and_log_q_match_oracle(oracle):
     b = _batch("qubo", [_sk(rng, n) for n in ns],
                [rng.integers(-2, 3, n).astype(np.float32) for n in ns],
                [0.2, 0.4, 0.8], 50)
-    prop = LearnedProposal(b, hidden=256, init_seed=5, init_flips=20.0)
+    prop = LearnedProposal(b, hidden=256, init_seed=5, init_flips=20.0,
+                           target_flips=target_flips)
     _perturb(prop, 2, 0.2)
     w = {k: prop.t[k].cpu().numpy().astype(np.float64)
          for k in ("w1", "b1", "w2", "b2")}
@@ -147,6 +144,7 @@ def test_flip_sampling_and_log_q_match_oracle(oracle):
     lqf = prop.sc_t["logq_fwd"].cpu().numpy()
     lqr = prop.sc_t["logq_rev"].cpu().numpy()
     checked = 0
+    nflips = []
     for i, n in enumerate(ns):
         for r in range(prop.B):
             c = rows[i, r]
@@ -159,6 +157,7 @@ def test_flip_sampling_and_log_q_match_oracle(oracle):
             _, z = mo.forward(x[None], w["w1"][i], w["b1"][i], w["w2"][i],
                               w["b2"][i])
             z = z[0, :n]
+            z = z + mo.flip_shift(z, target_flips)
             u = oracle.uniforms(seed, TAG_PROPOSAL, i, rnd, int(c), n)
             f_o = (u < mo.sigmoid(z)).astype(float)
             clear = np.abs(u - mo.sigmoid(z)) > 5e-3
@@ -170,9 +169,14 @@ def test_flip_sampling_and_log_q_match_oracle(oracle):
             xp[:n] = sp
             _, zr = mo.forward(xp[None], w["w1"][i], w["b1"][i], w["w2"][i],
                                w["b2"][i])
-            assert abs(lqr[i, r] - mo.log_q(zr[0, :n], flip[i, r, :n])) < 0.05
+            zr = zr[0, :n]
+            zr = zr + mo.flip_shift(zr, target_flips)
+            assert abs(lqr[i, r] - mo.log_q(zr, flip[i, r, :n])) < 0.05
+            nflips.append(flip[i, r].sum())
             checked += 1
     assert checked == 100
+    if target_flips > 0:
+        assert abs(np.mean(nflips) - target_flips) < 1.0
 
 
 @pytest.mark.parametrize("ptype", ["ising", "qubo"])

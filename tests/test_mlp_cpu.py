@@ -6,16 +6,12 @@ Boltzmann probabilities; a planted mistake (the reverse-proposal term left
 out) must fail the same check.
 """
 import ctypes
-import os
-import sys
 
 import numpy as np
 import pytest
 import torch
 
-from conftest import ROOT
-
-from oracle import mlp_oracle as mo  # noqa: E402
+from oracle import mlp_oracle as mo
 
 
 def _net(rng, B=6, n=8, H=16):
@@ -124,7 +120,7 @@ def test_mlp_structs_and_null_arguments():
     assert lib.pysa_gb_mlp_backward(None, None, None, None) == -1
     assert lib.pysa_gb_mlp_adam(None, 1e-3, 0.9, 0.999, 1e-8, 1, None) == -1
     assert lib.pysa_gb_propose(None, None, None, None, None, None, 1, None,
-                               0, 0, None, None) == -1
+                               0, 0, 0.0, None, None) == -1
     assert lib.pysa_gb_proposal_j_elems(2, 300, 1) < 0
     assert lib.pysa_gb_proposal_j_elems(2, 512, 2) == 2 * 2 * 512 * 512
     m = _lib.Mlp(1, 512, 1000, 128)   # hidden not a multiple of 256
