@@ -36,6 +36,10 @@ WORKLOADS = {
                             tmin=0.5, tmax=8.0, sweeps=2000, update="random"),
     "sk128": dict(kind="sk", n=128, replicas=32, reads=100, tmin=1.0,
                   tmax=3.5, sweeps=1000, update="sequential"),
+    # learned proposal vs plain PT, TTS(99%) (not an attempts/s line)
+    "sk512_tts": dict(kind="pm1", n=512, replicas=64, reads=128, tmin=0.3,
+                      tmax=3.0, instances=64, budgets=(1000, 4000, 16000),
+                      target_sweeps=32000, update="sequential"),
 }
 
 
@@ -152,6 +156,116 @@ def cpu_reference(w, ptype, P, reads, sweeps, nthreads=0):
     return reads * R * n * sweeps / dt, dt
 
 
+def run_tts_workload(args, w, rank, world):
+    """TTS(99%) of plain GPU PT against PT with the learned proposal on
+    seeded +-1 SK instances (J_ij = +-1 symmetric, zero diagonal).
+
+    Target energy of each instance: the lowest energy seen by a long plain
+    run (target_sweeps) or by any arm.  Each arm restarts from the same
+    random states for every sweep budget S; one run = one read, all
+    I x Rd reads run concurrently, so t_run = wall time / (I Rd) and
+    TTS = t_run ln(0.01) / ln(1 - p_s) (per instance; the line reports the
+    median over instances at the best budget).  The learned arm's wall time
+    includes its online training and proposals."""
+    if rank != 0:
+        return 0
+    import torch
+    from pysa_gb300 import Instance, PTBatch, pack_spins
+    from pysa_gb300.proposal import LearnedProposal, run_with_proposals
+    from pysa_gb300.tts import batch_tts
+    I, n, R, Rd = w["instances"], w["n"], w["replicas"], w["reads"]
+    rng = np.random.default_rng(2024)
+    Js = []
+    for _ in range(I):
+        J = np.triu(rng.choice([-1.0, 1.0], size=(n, n)), 1)
+        Js.append((J + J.T).astype(np.float32))
+    h0 = np.zeros(n, np.float32)
+    lad = np.sort(ladder(w)).astype(np.float32)
+    x0 = (2 * np.random.default_rng(7).integers(0, 2, (I * Rd * R, n)) - 1
+          ).astype(np.float32)
+
+    def fresh():
+        b = PTBatch("ising", [Instance(J, h0, lad, Rd) for J in Js])
+        b.set_states(pack_spins(x0, "ising", b.words))
+        torch.cuda.synchronize()
+        return b
+
+    def per_read_best(b):
+        return b.best_energy.view(I, Rd, R).min(dim=2).values.cpu().numpy()
+
+    sampler = ClockSampler(0)
+    with sampler:
+        b = fresh()
+        t0 = time.perf_counter()
+        b.run(w["target_sweeps"], seed=11)
+        torch.cuda.synchronize()
+        t_target = time.perf_counter() - t0
+        b.check_status()
+        target = per_read_best(b).min(axis=1)
+        del b
+        arms = {"plain": {}, "learned": {}}
+        stats = {}
+        for S in w["budgets"]:
+            b = fresh()
+            t0 = time.perf_counter()
+            b.run(S, seed=13)
+            torch.cuda.synchronize()
+            arms["plain"][S] = (time.perf_counter() - t0, per_read_best(b))
+            b.check_status()
+            del b
+            b = fresh()
+            prop = LearnedProposal(b, hidden=1024, lr=1e-3, init_seed=3,
+                                   target_flips=2.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = run_with_proposals(b, prop, S, seed=13, interval=10,
+                                    train_every=5, train_pairs=200_000,
+                                    min_train_steps=200, min_accept=0.01)
+            torch.cuda.synchronize()
+            arms["learned"][S] = (time.perf_counter() - t0, per_read_best(b))
+            b.check_status()
+            stats[S] = {"rounds": st.rounds, "train_steps": st.train_steps,
+                        "acceptance_mean": float(st.acceptance.mean()),
+                        "accepted_moves": int(st.accepted.sum()),
+                        "enabled_instances_at_end": int(st.enabled.sum())}
+            del b, prop
+    for arm in arms.values():
+        for S, (_, best) in arm.items():
+            target = np.minimum(target, best.min(axis=1))
+    out = {}
+    for name, arm in arms.items():
+        rows = {}
+        for S, (t, best) in arm.items():
+            r = batch_tts(best, target, t)
+            rows[S] = {"seconds": t, "tts_median_s": r["tts_median"],
+                       "p_success_mean": float(r["success_prob"].mean()),
+                       "solved_instances": r["solved_instances"]}
+        bestS = min(rows, key=lambda k: rows[k]["tts_median_s"])
+        out[name] = {"tts99_median_s": rows[bestS]["tts_median_s"],
+                     "best_budget_sweeps": bestS,
+                     "budgets": {str(k): v for k, v in rows.items()}}
+    line = {
+        "metric": "tts99_median_s", "value": out["learned"]["tts99_median_s"],
+        "unit": "s", "n_gpus": 1, "steps": len(w["budgets"]), "warmup": 0,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 sweeps; bf16/f32 network", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "instances": I, "n": n,
+                   "replicas": R, "reads": Rd, "tmin": w["tmin"],
+                   "tmax": w["tmax"], "budgets": list(w["budgets"]),
+                   "target_sweeps": w["target_sweeps"],
+                   "target_seconds": t_target,
+                   "network": "512-1024-512 per instance, target 2 flips, "
+                              "propose every 10 sweeps, train every 5 "
+                              "(2e5 pairs max), off below 1% acceptance "
+                              "after 200 training steps"},
+        "learned": out["learned"], "plain_gpu": out["plain"],
+        "proposal_stats": {str(k): v for k, v in stats.items()},
+        "clocks": sampler.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference_arm(args, w, rank, world):
     if rank != 0:
         return 0
@@ -205,6 +319,14 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if args.workload.endswith("_tts"):
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable":
+                                  "TTS workload compares two GPU arms; the "
+                                  "reference has no learned proposal"}))
+            return 0
+        return run_tts_workload(args, w, rank, world)
     if args.impl == "reference":
         return run_reference_arm(args, w, rank, world)
 

@@ -240,41 +240,64 @@ class LearnedProposal:
 
 def run_with_proposals(batch: PTBatch, prop: LearnedProposal | None,
                        num_sweeps: int, *, seed: int, interval: int = 10,
-                       train_pairs: int = 200_000, warmup_rounds: int = 20,
-                       min_accept: float = 0.01, use_pt: bool = True,
+                       train_every: int | None = None,
+                       train_pairs: int = 200_000, min_train_steps: int = 200,
+                       check_every: int = 20, min_accept: float = 0.01,
+                       use_pt: bool = True,
                        propose: bool = True) -> ProposalStats | None:
-    """num_sweeps sequential PT sweeps of `batch`, with (when prop is given)
-    after every `interval` sweeps: one training step on the cold-state pair
-    of every read until each instance has seen `train_pairs` pairs, then one
-    learned proposal per read.  After `warmup_rounds` proposal rounds an
-    instance whose acceptance rate is below `min_accept` stops proposing.
+    """num_sweeps sequential PT sweeps of `batch`.  With a network: every
+    `train_every` sweeps (default `interval`) one training step on the
+    same-chain pairs of every read, until each instance has seen
+    `train_pairs` pairs; every `interval` sweeps one learned proposal per
+    read.  Once the network has had `min_train_steps` steps, every
+    `check_every` proposal rounds an instance whose acceptance rate over
+    those rounds is below `min_accept` stops proposing for the rest of the
+    run (plain sweeps only); training stops when no instance proposes.
     Returns the proposal statistics (None without a network)."""
     if prop is None:
         batch.run(num_sweeps, seed=seed, use_pt=use_pt)
         return None
-    chunks = max(int(num_sweeps) // int(interval), 1)
+    interval = max(int(interval), 1)
+    train_every = interval if train_every is None else max(int(train_every), 1)
+    step = math.gcd(interval, train_every)
     st = prop.stats
     reads = np.asarray(batch.Rd, np.float64)
     max_steps = int(math.ceil(train_pairs / max(float(reads.min()), 1.0)))
     done = 0
-    for k in range(chunks):
-        todo = interval if k < chunks - 1 else int(num_sweeps) - done
+    win_rounds = 0
+    acc0 = prop.accepted.clone()
+
+    def settle():
+        nonlocal acc0, win_rounds
+        now = prop.accepted.clone()
+        acc = (now - acc0).cpu().numpy().astype(np.float64)
+        acc0 = now
+        st.accepted += acc
+        rate = acc / np.maximum(win_rounds * reads, 1.0)
+        win_rounds = 0
+        return rate
+
+    while done < int(num_sweeps):
+        todo = min(step, int(num_sweeps) - done)
         batch.run(todo, seed=seed, use_pt=use_pt, graph_chunk=0)
         done += todo
-        if st.train_steps < max_steps:
+        if (done % train_every == 0 and st.train_steps < max_steps
+                and st.enabled.any()):
             prop.observe()
-        if not propose or not st.enabled.any():
+        if not propose or done % interval or not st.enabled.any():
             continue
-        before = prop.accepted.clone()
         prop.propose(seed, st.rounds)
         st.rounds += 1
-        acc = (prop.accepted - before).cpu().numpy().astype(np.float64)
         st.proposed += reads * st.enabled
-        st.accepted += acc
-        if st.rounds >= warmup_rounds:
-            low = st.enabled & (st.acceptance < min_accept)
-            if low.any():
-                st.enabled &= ~low
-                prop.enabled.copy_(torch.from_numpy(
-                    st.enabled.astype(np.int32)))
+        win_rounds += 1
+        if win_rounds >= check_every:
+            rate = settle()
+            if st.train_steps >= min(min_train_steps, max_steps):
+                low = st.enabled & (rate < min_accept)
+                if low.any():
+                    st.enabled &= ~low
+                    prop.enabled.copy_(torch.from_numpy(
+                        st.enabled.astype(np.int32)))
+    if win_rounds:
+        settle()
     return st
