@@ -129,6 +129,13 @@ typedef struct {
   int32_t tc_enabled;       /* 1: sequential sweeps use the tensor cores */
   int32_t tc_variant_start[3]; /* host: items of fold F = 1, 2, 4 */
   int32_t tc_variant_count[3];
+  int32_t tc_min_n;         /* instances with tc_min_n <= n <= 2048 take the
+                               tensor-core sweep, the others the plain kernel
+                               in the same sweep (0 means 64) */
+  int32_t *tc_inst;         /* [num_instances] device flags written by
+                               pysa_gb_tc_setup: 1 = tensor-core instance */
+  int32_t plain_live;       /* host, from pysa_gb_tc_setup: bit v set when
+                               plain variant v still has instances */
   int32_t pad_;
 } pysa_gb_workspace;
 
@@ -181,12 +188,14 @@ int pysa_gb_setup(const pysa_gb_problems *p, const pysa_gb_host_tables *host,
                   pysa_gb_workspace *ws, void *stream);
 
 /* Tensor-core blocked sweep (sequential order, 64 <= n <= 2048): sizes of
- * tc_b, tc_diag and tc_items (int32 entries) for `terms` BF16 terms, and the
- * set-up that packs them.  Returns the number of tc work items, or
- * PYSA_GB_ERR_SIZE when an instance is outside the supported range. */
+ * tc_b, tc_diag and tc_items (int32 entries) for `terms` BF16 terms over the
+ * instances with min_n <= n <= 2048 (min_n < 64 means 64), and the set-up
+ * that packs them (instances selected by ws->tc_min_n; the others stay on
+ * the plain kernel, which skips the tensor-core instances in sequential
+ * sweeps).  Returns the number of tc work items. */
 int pysa_gb_tc_workspace(int32_t num_instances,
                          const pysa_gb_host_tables *host, int32_t terms,
-                         int64_t out[3]);
+                         int32_t min_n, int64_t out[3]);
 int pysa_gb_tc_setup(const pysa_gb_problems *p,
                      const pysa_gb_host_tables *host, pysa_gb_workspace *ws,
                      void *stream);

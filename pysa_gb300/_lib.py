@@ -45,6 +45,7 @@ class Workspace(ctypes.Structure):
                 ("tc_diag_elems", I64), ("tc_items", P),
                 ("tc_num_items", I32), ("tc_terms", I32), ("tc_enabled", I32),
                 ("tc_variant_start", I32 * 3), ("tc_variant_count", I32 * 3),
+                ("tc_min_n", I32), ("tc_inst", P), ("plain_live", I32),
                 ("pad_", I32)]
 
 
@@ -100,7 +101,7 @@ def load() -> ctypes.CDLL:
         "pysa_gb_last_error": ([], ctypes.c_char_p),
         "pysa_gb_workspace_bytes": ([I32, P, P], ctypes.c_int),
         "pysa_gb_setup": ([P, P, P, P], ctypes.c_int),
-        "pysa_gb_tc_workspace": ([I32, P, I32, P], ctypes.c_int),
+        "pysa_gb_tc_workspace": ([I32, P, I32, I32, P], ctypes.c_int),
         "pysa_gb_tc_setup": ([P, P, P, P], ctypes.c_int),
         "pysa_gb_prepare": ([P, P, P, I32, I32, I32, P], ctypes.c_int),
         "pysa_gb_sweeps": ([P, P, P, P, I32, P], ctypes.c_int),

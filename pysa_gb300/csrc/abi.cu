@@ -216,9 +216,13 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   return PYSA_GB_OK;
 }
 
+static inline bool tc_selected(int n, int min_n) {
+  return n >= (min_n < 64 ? 64 : min_n) && n <= 2048;
+}
+
 int pysa_gb_tc_workspace(int32_t num_instances,
                          const pysa_gb_host_tables* host, int32_t terms,
-                         int64_t out[3]) {
+                         int32_t min_n, int64_t out[3]) {
   if (num_instances < 0 || !out || (terms != 1 && terms != 2) ||
       (num_instances > 0 && (!host || !host->n || !host->replicas ||
                              !host->reads)))
@@ -226,8 +230,7 @@ int pysa_gb_tc_workspace(int32_t num_instances,
   int64_t b = 0, d = 0, items = 0;
   for (int i = 0; i < num_instances; ++i) {
     const int n = host->n[i];
-    if (n < 64 || n > 2048)
-      return fail(PYSA_GB_ERR_SIZE, "tensor-core sweep needs 64 <= n <= 2048");
+    if (!tc_selected(n, min_n)) continue;
     b += tc_b_elems(n, terms);
     d += tc_diag_elems(n);
     const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
@@ -245,19 +248,28 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   if (!p || !host || !ws || !host->chain_off || !host->j_off || !host->ld)
     return fail(PYSA_GB_ERR_ARG, "tc_setup: null argument");
   int64_t need[3];
-  const int items_n =
-      pysa_gb_tc_workspace(p->num_instances, host, ws->tc_terms, need);
+  const int min_n = ws->tc_min_n;
+  const int items_n = pysa_gb_tc_workspace(p->num_instances, host,
+                                           ws->tc_terms, min_n, need);
   if (items_n < 0) return items_n;
   if (!ws->tc_b || ws->tc_b_elems < need[0] || !ws->tc_diag ||
       ws->tc_diag_elems < need[1] || !ws->tc_items ||
-      ws->tc_num_items < items_n)
+      ws->tc_num_items < items_n || !ws->tc_inst)
     return fail(PYSA_GB_ERR_ARG, "tc workspace too small");
   cudaStream_t st = (cudaStream_t)stream;
   std::vector<int64_t> boff(p->num_instances), doff(p->num_instances);
+  std::vector<int32_t> flags(p->num_instances, 0);
+  const PlainItemPlan plan = make_item_plan();
   int64_t bo = 0, dd = 0;
+  int live = 0;
   for (int i = 0; i < p->num_instances; ++i) {
     boff[i] = bo;
     doff[i] = dd;
+    if (!tc_selected(host->n[i], min_n)) {
+      live |= 1 << plan.variant_of(host->n[i]);
+      continue;
+    }
+    flags[i] = 1;
     bo += tc_b_elems(host->n[i], ws->tc_terms);
     dd += tc_diag_elems(host->n[i]);
   }
@@ -266,7 +278,7 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   for (int v = 0; v < 3; ++v) {
     ws->tc_variant_start[v] = (int32_t)items.size();
     for (int i = 0; i < p->num_instances; ++i) {
-      if (tc_fold_for(host->n[i]) != folds[v]) continue;
+      if (!flags[i] || tc_fold_for(host->n[i]) != folds[v]) continue;
       const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
       const int cc = tc_chains_per_cta(host->n[i]);
       for (int64_t c = 0; c < chains; c += cc) {
@@ -288,12 +300,21 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "copy tc work list");
   }
+  if (p->num_instances > 0) {
+    cudaError_t e = cudaMemcpyAsync(ws->tc_inst, flags.data(),
+                                    flags.size() * sizeof(int32_t),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy tc instance flags");
+  }
   for (int i = 0; i < p->num_instances; ++i) {
+    if (!flags[i]) continue;
     cudaError_t e = launch_pack_tc(p->J + host->j_off[i], host->ld[i],
                                    host->n[i], ws->tc_terms, ws->tc_b + boff[i],
                                    ws->tc_diag + doff[i], st);
     if (e != cudaSuccess) return cuda_fail(e, "pack tc tiles");
   }
+  // host vectors above are pageable: the copies are complete on return
+  ws->plain_live = live;
   ws->tc_enabled = 1;
   return PYSA_GB_OK;
 }
@@ -331,9 +352,12 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   cudaStream_t st = (cudaStream_t)stream;
   int caps[kNumPlainVariants];
   const bool tc_path = ws->tc_enabled && !random && ws->tc_items;
+  // plain variants that run: all of them, or (tensor-core path) those with
+  // instances left to the plain kernel
+  const int plain_mask = tc_path ? ws->plain_live : 0xFF;
   for (int v = 0; v < kNumPlainVariants; ++v) {
     caps[v] = 0;
-    if (ws->variant_count[v] > 0 && !tc_path) {
+    if (ws->variant_count[v] > 0 && ((plain_mask >> v) & 1)) {
       const int rc = prepare_variant(v, random, &caps[v]);
       if (rc != PYSA_GB_OK) return rc;
     }
@@ -348,6 +372,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   a.perm_slots = ws->perm_slots > 0 ? ws->perm_slots : 1;
   a.update = o->update;
   a.seed = o->seed;
+  a.skip_inst = tc_path ? ws->tc_inst : nullptr;
   XArgs x;
   x.p = *p;
   x.s = *s;
@@ -385,10 +410,10 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
         if (e != cudaSuccess) return cuda_fail(e, "tc sweep launch");
       }
     }
-    for (int v = 0; !use_tc && (phases & 1) && v < kNumPlainVariants; ++v) {
+    for (int v = 0; (phases & 1) && v < kNumPlainVariants; ++v) {
       if (v == 0 && random) launch_perm(pa, st);
       const int count = ws->variant_count[v];
-      if (count == 0) continue;
+      if (count == 0 || !((plain_mask >> v) & 1)) continue;
       a.items = reinterpret_cast<const SweepItem*>(ws->items) +
                 ws->variant_start[v];
       a.num_items = count;

@@ -48,6 +48,7 @@ struct PlainArgs {
   int32_t num_items;
   int32_t update;
   uint64_t seed;
+  const int32_t* skip_inst;  // [num_instances] 1 = handled elsewhere; or null
 };
 
 // Wait bounded by wall time (about one second), then report and give up.
@@ -115,6 +116,7 @@ __global__ void __launch_bounds__(W * 32, 1)
   for (int it = blockIdx.x; it < a.num_items; it += gridDim.x) {
     const SweepItem item = a.items[it];
     const int inst = item.inst;
+    if (a.skip_inst && a.skip_inst[inst]) continue;  // uniform per CTA
     const int n = a.p.n[inst];
     const int words = (n + 31) >> 5;
     const int64_t chain_base = a.p.chain_off[inst];

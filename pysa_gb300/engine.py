@@ -64,9 +64,12 @@ class PTBatch:
     def __init__(self, problem_type: str, instances: list[Instance],
                  device: torch.device | str | None = None,
                  perm_slots: int = 1, kernel: str = "auto"):
-        """kernel: 'plain' (CUDA-core sweep), 'tc' (tensor-core blocked
-        sweep, sequential order, 64 <= n <= 2048) or 'auto' (tc when every
-        instance has 256 <= n <= 2048)."""
+        """kernel: 'plain' (CUDA-core sweep for every instance), 'tc'
+        (tensor-core blocked sweep for every instance, sequential order,
+        64 <= n <= 2048), 'auto' (tensor cores for the instances with
+        256 <= n <= 2048, the plain kernel for the rest, in the same sweep)
+        or 'autotune' ('auto' until autotune() picks the threshold by
+        timing; run() calls it on first use)."""
         if not torch.cuda.is_available():
             raise RuntimeError(
                 "pysa_gb300 needs a CUDA GPU: the sweeps run only as "
@@ -171,29 +174,93 @@ class PTBatch:
         check(self.lib.pysa_gb_setup(ref(self.p), ref(ht_), ref(self.ws),
                                      self._stream.cuda_stream), "setup")
         self._graphs = {}
+        self._ht = ht_
         self.tc = False
-        if kernel == "tc" or (kernel == "auto" and I and n.min() >= 256 and
-                              n.max() <= 2048):
-            terms = 1 if all(bf16_exact(x.J) for x in instances) else 2
+        self.tc_min_n = None
+        if kernel == "tc":
+            if I and (n.min() < 64 or n.max() > 2048):
+                raise ValueError("kernel='tc' needs 64 <= n <= 2048 for "
+                                 "every instance")
+            self._setup_tc(64)
+        elif kernel in ("auto", "autotune"):
+            if I and ((n >= 256) & (n <= 2048)).any():
+                self._setup_tc(256)
+        elif kernel != "plain":
+            raise ValueError(f"unknown kernel {kernel!r}")
+        self.autotune_pending = kernel == "autotune"
+
+    def _setup_tc(self, min_n: int | None):
+        """Select the tensor-core sweep for instances with
+        min_n <= n <= 2048 (None: plain kernel for every instance)."""
+        I = len(self.instances)
+        if min_n is None:
+            self.ws.tc_enabled = 0
+            self.tc = False
+            self.tc_min_n = None
+            return
+        ht_ = self._ht
+        if not hasattr(self, "tc_b"):
+            # sized once for the widest selection (every instance >= 64)
+            terms = 1 if all(bf16_exact(x.J) for x in self.instances) else 2
             tneed = (ctypes.c_int64 * 3)()
-            titems = check(self.lib.pysa_gb_tc_workspace(I, ref(ht_), terms,
-                                                         tneed), "tc sizing")
-            self.tc_b = z(max(int(tneed[0]), 1), dt=torch.int16)
-            self.tc_diag = z(max(int(tneed[1]), 1), dt=torch.float32)
-            self.tc_items = z(max(int(tneed[2]), 8), dt=torch.int32)
+            titems = check(self.lib.pysa_gb_tc_workspace(
+                I, ref(ht_), terms, 64, tneed), "tc sizing")
+            z = lambda k, dt: torch.zeros(k, dtype=dt, device=self.device)
+            self.tc_b = z(max(int(tneed[0]), 1), torch.int16)
+            self.tc_diag = z(max(int(tneed[1]), 1), torch.float32)
+            self.tc_items = z(max(int(tneed[2]), 8), torch.int32)
+            self.tc_inst = z(max(I, 1), torch.int32)
             self.ws.tc_b = _ptr(self.tc_b)
             self.ws.tc_b_elems = int(tneed[0])
             self.ws.tc_diag = _ptr(self.tc_diag)
             self.ws.tc_diag_elems = int(tneed[1])
             self.ws.tc_items = _ptr(self.tc_items)
             self.ws.tc_num_items = max(titems, 1)
+            self.ws.tc_inst = _ptr(self.tc_inst)
             self.ws.tc_terms = terms
-            check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(ht_),
-                                            ref(self.ws),
-                                            self._stream.cuda_stream),
-                  "tc setup")
-            self.tc = True
             self.tc_terms = terms
+        self.ws.tc_min_n = int(min_n)
+        check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(ht_), ref(self.ws),
+                                        self._stream.cuda_stream), "tc setup")
+        self._graphs = {}
+        self.tc = True
+        self.tc_min_n = int(min_n)
+
+    def autotune(self, sweeps: int = 3, candidates=(64, 256, 512, 1024, None),
+                 seed: int = 1) -> dict:
+        """Choose the tensor-core threshold (instances with n >= threshold
+        take the tensor-core sweep, the rest the plain kernel; None = plain
+        only) by timing `sweeps` sequential sweeps of the current chains per
+        candidate with CUDA events.  The chains are restored afterwards, so
+        results do not depend on the tuning.  Returns {candidate: ms}."""
+        self.autotune_pending = False
+        keep = [self.spins, self.energies, self.beta_idx, self.chain_beta,
+                self.best_energy, self.best_sweep, self.best_spins,
+                self.sweep_counter, self.status, self.ticket, self.fields]
+        saved = [t.clone() for t in keep]
+        n = np.asarray(self.n)
+        times = {}
+        for c in candidates:
+            if c is not None and not ((n >= max(c, 64)) & (n <= 2048)).any():
+                continue
+            self._setup_tc(c)
+            self.run(1, seed=seed, graph_chunk=0)   # warm-up, attributes
+            st = self._stream
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            self.run(sweeps, seed=seed, graph_chunk=0)
+            b.record(st)
+            b.synchronize()
+            times[c] = a.elapsed_time(b) / sweeps
+            for t, v in zip(keep, saved):
+                t.copy_(v)
+        best = min(times, key=times.get)
+        self._setup_tc(best)
+        torch.cuda.synchronize(self.device)
+        self.autotune_pending = False
+        self.autotune_ms = times
+        return times
 
     # ------------------------------------------------------------ states
     def set_states(self, spins_words: np.ndarray, energies=None,
@@ -228,6 +295,8 @@ class PTBatch:
         rebuilds fields and energies from the spins every that many sweeps
         (default 4 when J is not exact in BF16, never otherwise); the
         returned energies are then recomputed once more at the end."""
+        if self.autotune_pending and update == "sequential" and num_sweeps:
+            self.autotune()
         if recompute_every is None:
             recompute_every = 4 if (self.tc and self.tc_terms == 2) else 0
         upd = _lib.RANDOM if update == "random" else _lib.SEQUENTIAL

@@ -125,3 +125,45 @@ def test_tc_recompute_keeps_integer_trajectory(oracle, every):
     sp = unpack_spins(got["spins"].reshape(Rd, R, -1), n, "qubo", np.float32)
     assert (sp == want["spins"]).all()
     assert (got["energies"].reshape(Rd, R) == want["energies"]).all()
+
+
+@pytest.mark.parametrize("kernel", ["auto", "autotune"])
+def test_mixed_tc_and_plain_batch_bit_exact(oracle, kernel):
+    """One batch where instances with n >= 256 take the tensor-core sweep
+    and the others the plain kernel in the same sweep (kernel='auto'), or
+    whatever split the autotuner picks: every instance must still follow
+    the oracle bit for bit, and tuning must not change the chains."""
+    from pysa_gb300 import Instance, PTBatch, pack_spins, unpack_spins
+    rng = np.random.default_rng(31)
+    sizes, R, Rd, S = [100, 300, 40, 700, 1300], 4, 3, 12
+    insts, x0s = [], []
+    for n in sizes:
+        J, h = _int_qubo(rng, n)
+        betas = (1.0 / np.geomspace(0.5, 8.0, R)).astype(np.float32)
+        insts.append(Instance(J, h, betas, Rd))
+        x0s.append(rng.integers(0, 2, (Rd, R, n)).astype(np.float32))
+    b = PTBatch("qubo", insts, kernel=kernel)
+    assert b.tc and b.tc_min_n == 256
+    words = b.words
+    b.set_states(np.concatenate([pack_spins(x, "qubo", words).reshape(-1, words)
+                                 for x in x0s]), None)
+    b.run(S, seed=5)
+    if kernel == "autotune":
+        assert set(b.autotune_ms) >= {64, 256, None}
+    got = b.fetch()
+    c0 = 0
+    for i, (inst, x0) in enumerate(zip(insts, x0s)):
+        n = len(inst.h)
+        e0 = np.array([[oracle.energy64(inst.J, inst.h, s) for s in r]
+                       for r in x0], np.float32)
+        want = oracle.pt_run("qubo", inst.J, inst.h, inst.ladder, x0, e0,
+                             np.tile(np.arange(R, dtype=np.int32), (Rd, 1)),
+                             seed=5, num_sweeps=S, inst=i)
+        sl = slice(c0, c0 + R * Rd)
+        sp = unpack_spins(got["spins"][sl].reshape(Rd, R, words), n, "qubo",
+                          np.float32)
+        assert (sp == want["spins"]).all(), f"instance {i} (n={n})"
+        assert (got["energies"][sl].reshape(Rd, R) == want["energies"]).all()
+        assert (got["best_energy"][sl].reshape(Rd, R)
+                == want["best_energy"]).all()
+        c0 += R * Rd
