@@ -244,12 +244,13 @@ class PTBatch:
             if c is not None and not ((n >= max(c, 64)) & (n <= 2048)).any():
                 continue
             self._setup_tc(c)
-            self.run(1, seed=seed, graph_chunk=0)   # warm-up, attributes
+            self.run(1, seed=seed, graph_chunk=0,
+                     final_recompute=False)   # warm-up, attributes
             st = self._stream
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(st)
-            self.run(sweeps, seed=seed, graph_chunk=0)
+            self.run(sweeps, seed=seed, graph_chunk=0, final_recompute=False)
             b.record(st)
             b.synchronize()
             times[c] = a.elapsed_time(b) / sweeps
@@ -290,11 +291,14 @@ class PTBatch:
     # ------------------------------------------------------------ sweeps
     def run(self, num_sweeps: int, *, seed: int, update: str = "sequential",
             use_pt: bool = True, log_omega: bool = False,
-            graph_chunk: int = 64, recompute_every: int | None = None):
+            graph_chunk: int = 64, recompute_every: int | None = None,
+            final_recompute: bool = True):
         """Sweeps with exchange.  recompute_every: the tensor-core path
         rebuilds fields and energies from the spins every that many sweeps
-        (default 4 when J is not exact in BF16, never otherwise); the
-        returned energies are then recomputed once more at the end."""
+        (default 4 when J is not exact in BF16, never otherwise); with
+        final_recompute the returned energies are then recomputed once more
+        at the end (callers chaining many short runs can skip it and call
+        recompute() once)."""
         if self.autotune_pending and update == "sequential" and num_sweeps:
             self.autotune()
         if recompute_every is None:
@@ -331,12 +335,17 @@ class PTBatch:
             check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s),
                                           ref(self.ws), ref(opts), remaining,
                                           st), "sweeps")
-        if recompute_every and upd == _lib.SEQUENTIAL and self.tc:
-            # final fields and energies from the spins (f64-accumulated)
-            check(self.lib.pysa_gb_prepare(ref(self.p), ref(self.s),
-                                           ref(self.ws), 1, 0,
-                                           int(self.best_global), st),
-                  "final recompute")
+        if (final_recompute and recompute_every and upd == _lib.SEQUENTIAL
+                and self.tc):
+            self.recompute()
+
+    def recompute(self):
+        """Fields and energies of every chain from its spins (f32 partial
+        sums accumulated in f64); best_* untouched."""
+        check(self.lib.pysa_gb_prepare(ref(self.p), ref(self.s), ref(self.ws),
+                                       1, 0, int(self.best_global),
+                                       self._stream.cuda_stream),
+              "recompute")
 
     def check_status(self):
         code = int(self.status.item())

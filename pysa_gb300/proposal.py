@@ -279,7 +279,8 @@ def run_with_proposals(batch: PTBatch, prop: LearnedProposal | None,
 
     while done < int(num_sweeps):
         todo = min(step, int(num_sweeps) - done)
-        batch.run(todo, seed=seed, use_pt=use_pt, graph_chunk=0)
+        batch.run(todo, seed=seed, use_pt=use_pt, graph_chunk=0,
+                  final_recompute=False)
         done += todo
         if (done % train_every == 0 and st.train_steps < max_steps
                 and st.enabled.any()):
@@ -300,4 +301,6 @@ def run_with_proposals(batch: PTBatch, prop: LearnedProposal | None,
                         st.enabled.astype(np.int32)))
     if win_rounds:
         settle()
+    if batch.tc and batch.tc_terms == 2:
+        batch.recompute()
     return st
