@@ -109,7 +109,8 @@ typedef struct {
 /* Per-call workspace, caller-allocated (sizes from pysa_gb_workspace_bytes). */
 typedef struct {
   float *fields;          /* local fields, [num_chains, field_ld] */
-  int32_t field_ld;       /* row stride of fields (>= 32 * ceil(max_n/32)) */
+  int32_t field_ld;       /* row stride of fields (>= 32 * ceil(max_n/32),
+                             a multiple of 4; fields 16-byte aligned) */
   int32_t perm_slots;     /* visiting orders held (sweeps per batch) */
   int32_t *perm;          /* [perm_slots, num_instances, max_n] */
   float *packed_j;        /* couplings in the sweep kernel's row layout */

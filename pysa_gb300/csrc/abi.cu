@@ -163,8 +163,10 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     return fail(PYSA_GB_ERR_ARG, "packed_j too small");
   if (!ws->items || ws->num_items < items_n)
     return fail(PYSA_GB_ERR_ARG, "items too small");
-  if (ws->field_ld < need[2])
-    return fail(PYSA_GB_ERR_ARG, "field_ld too small");
+  if (ws->field_ld < need[2] || ws->field_ld % 4 != 0)
+    return fail(PYSA_GB_ERR_ARG, "field_ld too small or not a multiple of 4");
+  if (reinterpret_cast<uintptr_t>(ws->fields) % 16 != 0)
+    return fail(PYSA_GB_ERR_ARG, "fields must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   // work list ordered by variant; host-side ranges stored in the workspace
   std::vector<SweepItem> items;
@@ -349,6 +351,10 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
     return fail(PYSA_GB_ERR_ARG, "random order needs a perm workspace");
   if (o->log_omega_stride > 0 && !s->log_omega)
     return fail(PYSA_GB_ERR_ARG, "log_omega buffer missing");
+  if (ws->field_ld % 4 != 0 || reinterpret_cast<uintptr_t>(ws->fields) % 16)
+    return fail(PYSA_GB_ERR_ARG,
+                "fields: row stride must be a multiple of 4 floats and the "
+                "base 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   int caps[kNumPlainVariants];
   const bool tc_path = ws->tc_enabled && !random && ws->tc_items;

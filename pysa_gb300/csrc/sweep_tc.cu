@@ -82,6 +82,14 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
 __device__ __forceinline__ void stamp(const TcArgs& a, int t, int slot) {
   if (a.trace && blockIdx.x == 0) a.trace[t * 24 + slot] = globaltimer_ns();
 }
+// Row t (= number of blocks) holds whole-CTA marks: slots 0-5 for CTA 0
+// (entry, set-up done, last MMA done, fields stored, exit, field load
+// start), slots 8-13 the same for the last CTA of the grid.
+__device__ __forceinline__ void stamp_cta(const TcArgs& a, int t, int slot) {
+  if (!a.trace) return;
+  if (blockIdx.x == 0) a.trace[t * 24 + slot] = globaltimer_ns();
+  if (blockIdx.x == gridDim.x - 1) a.trace[t * 24 + 8 + slot] = globaltimer_ns();
+}
 
 // Named barriers in inline PTX: the warp is reconverged first and the
 // non-aligned barrier.sync form is used, since the compiler does not insert
@@ -152,6 +160,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   const bool rc = a.recompute_every > 0 && (sweep % a.recompute_every) == 0;
 
   // ---------------------------------------------------------------- set-up
+  if (threadIdx.x == 0) stamp_cta(a, NB, 0);
   if (warp == 0) {
     tc::tmem_alloc(sh.tmem_slot, ncols);
     tc::tmem_relinquish();
@@ -187,20 +196,66 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   const int64_t chain = item.chain0 + c;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 
+  // Field rows move between HBM and TMEM through a per-warp shared-memory
+  // transpose (in the B ring, idle before the producer starts and after the
+  // last MMA): the warp reads 4 rows x 128 B per instruction, coalesced,
+  // then each thread takes its own row.
+  float* stg = reinterpret_cast<float*>(smem + C::B_OFF) + warp * (32 * 33);
+  const int w_c0 = (32 * warp) % CC, w_q = (32 * warp) / CC;
+  if (threadIdx.x == 0) stamp_cta(a, NB, 5);
   if (warp < 4 && !rc) {  // local fields -> TMEM
-    for (int j0 = 0; j0 < S; j0 += 32) {
-      float v[32];
-      const float* f = a.fields + chain * a.field_ld + q * S + j0;
+    // two 32-column chunks per round: 16 independent 16-byte loads in flight
+    auto load4 = [&](int j0, int it) {
+      const int col = w_q * S + j0 + 4 * (lane & 7);
+      const int cr = w_c0 + 4 * it + (lane >> 3);
+      float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (j0 < S && cr < item.nchains) {
+        const float* f =
+            a.fields + (item.chain0 + cr) * (int64_t)a.field_ld + col;
+        if (col + 4 <= n) {
+          v = *reinterpret_cast<const float4*>(f);
+        } else {
+          v.x = col < n ? f[0] : 0.0f;
+          v.y = col + 1 < n ? f[1] : 0.0f;
+          v.z = col + 2 < n ? f[2] : 0.0f;
+        }
+      }
+      return v;
+    };
+    for (int j0 = 0; j0 < S; j0 += 64) {
+      float4 va[8], vb[8];
 #pragma unroll
-      for (int i = 0; i < 32; ++i)
-        v[i] = (valid && q * S + j0 + i < n) ? f[i] : 0.0f;
-      tc::tmem_st32(taddr + lane_base + j0, v);
+      for (int it = 0; it < 8; ++it) {
+        va[it] = load4(j0, it);
+        vb[it] = load4(j0 + 32, it);
+      }
+#pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2) {
+        if (j0 + 32 * h2 >= S) break;
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+          const float4 v = h2 ? vb[it] : va[it];
+          float* d = stg + (4 * it + (lane >> 3)) * 33 + 4 * (lane & 7);
+          d[0] = v.x;
+          d[1] = v.y;
+          d[2] = v.z;
+          d[3] = v.w;
+        }
+        __syncwarp();
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = stg[lane * 33 + i];
+        __syncwarp();
+        tc::tmem_st32(taddr + lane_base + j0 + 32 * h2, v);
+      }
     }
     tc::tmem_wait_st();
+    fence_proxy_async();
     tc::fence_before_sync();
   }
   __syncthreads();
   tc::fence_after_sync();
+  if (threadIdx.x == 0) stamp_cta(a, NB, 1);
 
   const uint32_t idesc_full = tc::idesc_bf16(128, 256);
 
@@ -336,7 +391,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) hsave[j] = hs[j];
           bool unc = false;
-          uint32_t pkg[8];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int k = 16 * g + j;
@@ -356,8 +410,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                                           : (sbit ? -1.0f : 1.0f))
                                  : 0.0f;
             dl_s[k * CC + c] = dl;
-            const uint32_t b16 = bf16_bits(dl);
-            if (j & 1) pkg[j >> 1] |= b16 << 16; else pkg[j >> 1] = b16;
             dEb = acc ? dEb - dn : dEb;
             wcur ^= acc ? (1u << (sb + j)) : 0u;
             if (j < 15) {  // exact corrections inside the sub-block
@@ -395,8 +447,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                                             : (sbit ? -1.0f : 1.0f))
                                    : 0.0f;
               dl_s[k * CC + c] = dl;
-              const uint32_t b16 = bf16_bits(dl);
-              if (j & 1) pkg[j >> 1] |= b16 << 16; else pkg[j >> 1] = b16;
               if (acc) {
                 dEb -= dn;
                 wcur ^= 1u << (sb + j);
@@ -416,26 +466,35 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             }
           }
           if (g < 2) w0 = wcur; else w1 = wcur;
-          // this sub-block's deltas into the A rows (chunks 2g, 2g+1); A is
-          // single-buffered, so the previous block's MMAs must be done
-          if (g == 0 && t > 0) {
-            if (lead) stamp(a, t, 2);
-            a_ok = tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
-            if (lead) stamp(a, t, 3);
-          }
+          if (lead) stamp(a, t, 10 + 3 * g);
+        }
+        // the block's deltas (kept in dl_s) into the A rows; A is
+        // single-buffered, so the previous block's MMAs must be done (they
+        // normally finished while this block was being decided)
+        if (t > 0) {
+          if (lead) stamp(a, t, 2);
+          a_ok = tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
+          if (lead) stamp(a, t, 3);
+        }
+        if (a_ok) {
+#pragma unroll 1
+          for (int g = 0; g < 4; ++g) {
+            uint32_t pkg[8];
 #pragma unroll
-          for (int qq = 0; qq < F; ++qq) {
-            const int m = qq * CC + c;
-            unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                  ((m >> 3) * 8) * 128 + (m & 7) * 16;
-            if (a_ok) {
+            for (int j = 0; j < 16; j += 2)
+              pkg[j >> 1] = bf16_bits(dl_s[(16 * g + j) * CC + c]) |
+                            (bf16_bits(dl_s[(16 * g + j + 1) * CC + c]) << 16);
+#pragma unroll
+            for (int qq = 0; qq < F; ++qq) {
+              const int m = qq * CC + c;
+              unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                    ((m >> 3) * 8) * 128 + (m & 7) * 16;
               *reinterpret_cast<uint4*>(rowp + (2 * g) * 128) =
                   make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
               *reinterpret_cast<uint4*>(rowp + (2 * g + 1) * 128) =
                   make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
             }
           }
-          if (lead) stamp(a, t, 10 + 3 * g);
         }
         if (valid) {
           spins_s[(2 * t) * CC + c] = w0;
@@ -457,20 +516,38 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     if (!*sh.abort && NB > 0)
       tc_wait(sh.mma_done, (NB - 1) & 1, sh, status);
     tc::fence_after_sync();
+    if (threadIdx.x == 0) stamp_cta(a, NB, 2);
     if (__all_sync(0xffffffffu, !*sh.abort)) {
       for (int j0 = 0; j0 < S; j0 += 32) {
         float v[32];
         tc::tmem_ld32(taddr + lane_base + j0, v);
-        float* f = a.fields + chain * a.field_ld + q * S + j0;
-        if (valid) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i)
-            if (q * S + j0 + i < n) f[i] = v[i];
+        for (int i = 0; i < 32; ++i) stg[lane * 33 + i] = v[i];
+        __syncwarp();
+        const int col = w_q * S + j0 + 4 * (lane & 7);
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+          const int rr = 4 * it + (lane >> 3);
+          const int cr = w_c0 + rr;
+          if (cr < item.nchains && col < n) {
+            const float* sv = stg + rr * 33 + 4 * (lane & 7);
+            float* f = a.fields + (item.chain0 + cr) * (int64_t)a.field_ld + col;
+            if (col + 4 <= n) {
+              *reinterpret_cast<float4*>(f) =
+                  make_float4(sv[0], sv[1], sv[2], sv[3]);
+            } else {
+              f[0] = sv[0];
+              if (col + 1 < n) f[1] = sv[1];
+              if (col + 2 < n) f[2] = sv[2];
+            }
+          }
         }
+        __syncwarp();
       }
     }
     tc::fence_before_sync();
     named_sync_128();
+    if (threadIdx.x == 0) stamp_cta(a, NB, 3);
     if (q == 0 && valid && !*sh.abort) {
       const float e_new = (float)(e0_s[c] + dE_s[c]);
       a.s.energies[chain] = e_new;
@@ -522,40 +599,67 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
         if (!ok) break;
         tc::commit(sh.rc_done);
       }
+      // rows [r_lo, r_hi) of the 256-row B tile in `slot` against A slice
+      // qq, into the field columns 256 j + r_lo ...
+      auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi) {
+        if (r_hi <= r_lo) return;
+        const uint32_t idesc =
+            r_hi - r_lo == 256 ? idesc_full : tc::idesc_bf16(128, r_hi - r_lo);
+        const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
+        const uint32_t b0 = smem_base +
+                            (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
+                            (uint32_t)(r_lo / 8) * 1024u;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks)
+          tc::mma_bf16(taddr + 256 * j + r_lo,
+                       tc::smem_desc(a0 + 256 * ks, 128, 1024),
+                       tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc, 1u);
+      };
       for (int t = 0; t < NB; ++t) {
         if (!tc_wait(sh.a_full, t & 1, sh, status)) break;
         stamp(a, t, 5);
         tc::fence_after_sync();
-        const int jf = (t + 1 < NB) ? ((64 * (t + 1)) % S) / 256 : 0;
+        // the next block's 64 columns: slice qn, tile jf, rows r0 .. r0+63
+        const bool has_next = t + 1 < NB;
+        const int cn = has_next ? (64 * (t + 1)) % S : 0;
+        const int qn = has_next ? (64 * (t + 1)) / S : 0;
+        const int jf = cn / 256, r0 = cn % 256;
         bool ok = true;
         for (int jj = 0; jj < NT && ok; ++jj) {
           const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
           const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-          const uint32_t idesc =
-              width == 256 ? idesc_full : tc::idesc_bf16(128, width);
-          for (int term = 0; term < T && ok; ++term) {
-            for (int qq = 0; qq < F; ++qq) {
-              const uint32_t slot = u % C::NS;
-              if (!tc_wait(&sh.full[slot], (u / C::NS) & 1, sh, status)) {
+          // stage order: slices from qn on, terms inside (the producer
+          // issues the same order)
+          for (int k = 0; k < F && ok; ++k) {
+            const int qq = (qn + k) % F;
+            const bool crit = jj == 0 && k == 0 && has_next;
+            for (int term = 0; term < T; ++term) {
+              const uint32_t slot = (u + term) % C::NS;
+              if (!tc_wait(&sh.full[slot], ((u + term) / C::NS) & 1, sh,
+                           status)) {
                 ok = false;
                 break;
               }
               tc::fence_after_sync();
-              const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
-              const uint32_t b0 =
-                  smem_base + (uint32_t)(C::B_OFF + slot * C::B_STAGE);
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks)
-                tc::mma_bf16(taddr + 256 * j,
-                             tc::smem_desc(a0 + 256 * ks, 128, 1024),
-                             tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc, 1u);
-              tc::commit(&sh.free_[slot]);
-              ++u;
+              if (crit)
+                mma_rows(slot, qq, j, r0, r0 + 64);
+              else
+                mma_rows(slot, qq, j, 0, width);
             }
-          }
-          if (jj == 0 && t + 1 < NB) {
-            tc::commit(sh.h_ready);
-            stamp(a, t, 6);
+            if (!ok) break;
+            if (crit) {
+              // the next block's decisions may start once these land
+              tc::commit(sh.h_ready);
+              stamp(a, t, 6);
+              for (int term = 0; term < T; ++term) {
+                const uint32_t slot = (u + term) % C::NS;
+                mma_rows(slot, qq, j, 0, r0);
+                mma_rows(slot, qq, j, r0 + 64, width);
+              }
+            }
+            for (int term = 0; term < T; ++term)
+              tc::commit(&sh.free_[(u + term) % C::NS]);
+            u += T;
           }
         }
         if (!ok) break;
@@ -603,18 +707,24 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
         if (!ok) break;
       }
       for (int t = 0; t < NB && !*sh.abort; ++t) {
-        if (t >= 2) {
-          if (!tc_wait(&sh.jbb_free[t & 1], ((t >> 1) - 1) & 1, sh, status))
+        // the next block's diagonal block, into the buffer block t-1 used:
+        // it lands while block t is being decided
+        if (t >= 1 && t + 1 < NB) {
+          if (!tc_wait(&sh.jbb_free[(t + 1) & 1], (((t + 1) >> 1) - 1) & 1,
+                       sh, status))
             break;
-          issue_jbb(t);
+          issue_jbb(t + 1);
         }
-        const int jf = (t + 1 < NB) ? ((64 * (t + 1)) % S) / 256 : 0;
+        const bool has_next = t + 1 < NB;
+        const int jf = has_next ? ((64 * (t + 1)) % S) / 256 : 0;
+        const int qn = has_next ? (64 * (t + 1)) / S : 0;
         bool ok = true;
         for (int jj = 0; jj < NT && ok; ++jj) {
           const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
           const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-          for (int term = 0; term < T && ok; ++term) {
-            for (int qq = 0; qq < F; ++qq) {
+          for (int k = 0; k < F && ok; ++k) {
+            const int qq = (qn + k) % F;
+            for (int term = 0; term < T; ++term) {
               const uint32_t slot = u % C::NS;
               if (u >= (uint32_t)C::NS &&
                   !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh,
@@ -667,6 +777,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   __syncwarp();  // single-lane roles (MMA, producer) rejoin their warps
   tc::fence_before_sync();
   __syncthreads();
+  if (threadIdx.x == 0) stamp_cta(a, NB, 4);
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(taddr, ncols);
