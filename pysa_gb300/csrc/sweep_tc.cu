@@ -47,7 +47,12 @@ struct TcCfg {
   static constexpr size_t E0_OFF = DE_OFF + (size_t)CC * 8;
   static constexpr size_t EPART_OFF = E0_OFF + (size_t)CC * 8;
   static constexpr size_t BETA_OFF = EPART_OFF + (size_t)F * CC * 8;
-  static constexpr size_t BAR_OFF = (BETA_OFF + CC * 4 + 63) / 64 * 64;
+  // F == 2: corrections of sub-blocks 2 and 3 from the older sub-blocks,
+  // computed by the idle slice's threads ([2][16][CC] floats)
+  static constexpr bool HELP = F == 2;
+  static constexpr size_t CORR_OFF = BETA_OFF + CC * 4;
+  static constexpr size_t CORR_BYTES = HELP ? (size_t)2 * 16 * CC * 4 : 0;
+  static constexpr size_t BAR_OFF = (CORR_OFF + CORR_BYTES + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
   // lf_full[2], lf_free[2], full[NS], free[NS]
   static constexpr int NBARS = 13 + 2 * NS;
@@ -99,6 +104,12 @@ __device__ __forceinline__ void named_sync_128() {
   asm volatile("barrier.sync 1, 128;" ::: "memory");
 }
 
+// Deciding and helping threads of the four decision warps (fold 2).
+__device__ __forceinline__ void named_sync_dec() {
+  __syncwarp();
+  asm volatile("barrier.sync 3, 128;" ::: "memory");
+}
+
 __device__ __forceinline__ void named_sync_helpers() {
   __syncwarp();
   asm volatile("barrier.sync 2, 64;" ::: "memory");
@@ -137,6 +148,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
   float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
   float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
+  float* corr_s = reinterpret_cast<float*>(smem + C::CORR_OFF);
   const uint32_t smem_base = smem_addr(smem);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -366,8 +378,15 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           float hs[16];
           tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
           if (lead) stamp(a, t, 8 + 3 * g);
+          // with helpers, sub-blocks older than g-1 arrive precomputed
+          const int k_lo = (C::HELP && g >= 2) ? 16 * (g - 1) : 0;
+          if (C::HELP && g >= 2) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              hs[j] += corr_s[((g - 2) * 16 + j) * CC + c];
+          }
 #pragma unroll 2
-          for (int k = 0; k < 16 * g; ++k) {
+          for (int k = k_lo; k < 16 * g; ++k) {
             const float d = dl_s[k * CC + c];
             const float4* jr =
                 reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
@@ -467,6 +486,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           }
           if (g < 2) w0 = wcur; else w1 = wcur;
           if (lead) stamp(a, t, 10 + 3 * g);
+          if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
         }
         // the block's deltas (kept in dl_s) into the A rows; A is
         // single-buffered, so the previous block's MMAs must be done (they
@@ -502,6 +522,60 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           dE_s[c] += (double)dEb;
         }
         fence_proxy_async();
+      } else if (C::HELP) {
+        // helper (the other slice's thread of chain c), or a deciding
+        // thread after an abort: same three barriers as the deciding path
+        const bool hgo = __all_sync(0xffffffffu, !*sh.abort) && q != qt;
+        const float* jb = jbb + (t & 1) * 4096;
+        float c3[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) c3[j] = 0.0f;
+        named_sync_dec();  // sub-block 0 decided
+        bool hok = hgo && valid &&
+                   tc_wait(&sh.jbb_full[t & 1], (t >> 1) & 1, sh, status);
+        if (hok) {
+          float c2[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) c2[j] = 0.0f;
+#pragma unroll 2
+          for (int k = 0; k < 16; ++k) {
+            const float d = dl_s[k * CC + c];
+            const float4* jr = reinterpret_cast<const float4*>(jb + k * 64);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+              const float4 v2 = jr[8 + q4], v3 = jr[12 + q4];
+              c2[4 * q4 + 0] = fmaf(d, v2.x, c2[4 * q4 + 0]);
+              c2[4 * q4 + 1] = fmaf(d, v2.y, c2[4 * q4 + 1]);
+              c2[4 * q4 + 2] = fmaf(d, v2.z, c2[4 * q4 + 2]);
+              c2[4 * q4 + 3] = fmaf(d, v2.w, c2[4 * q4 + 3]);
+              c3[4 * q4 + 0] = fmaf(d, v3.x, c3[4 * q4 + 0]);
+              c3[4 * q4 + 1] = fmaf(d, v3.y, c3[4 * q4 + 1]);
+              c3[4 * q4 + 2] = fmaf(d, v3.z, c3[4 * q4 + 2]);
+              c3[4 * q4 + 3] = fmaf(d, v3.w, c3[4 * q4 + 3]);
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) corr_s[j * CC + c] = c2[j];
+        }
+        named_sync_dec();  // sub-block 1 decided; corrections of 2 out
+        if (hok) {
+#pragma unroll 2
+          for (int k = 16; k < 32; ++k) {
+            const float d = dl_s[k * CC + c];
+            const float4* jr = reinterpret_cast<const float4*>(jb + k * 64);
+#pragma unroll
+            for (int q4 = 0; q4 < 4; ++q4) {
+              const float4 v3 = jr[12 + q4];
+              c3[4 * q4 + 0] = fmaf(d, v3.x, c3[4 * q4 + 0]);
+              c3[4 * q4 + 1] = fmaf(d, v3.y, c3[4 * q4 + 1]);
+              c3[4 * q4 + 2] = fmaf(d, v3.z, c3[4 * q4 + 2]);
+              c3[4 * q4 + 3] = fmaf(d, v3.w, c3[4 * q4 + 3]);
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) corr_s[(16 + j) * CC + c] = c3[j];
+        }
+        named_sync_dec();  // sub-block 2 decided; corrections of 3 out
       }
       if (lane == 0) stamp(a, t, 20 + warp);
       named_sync_128();
