@@ -137,6 +137,12 @@ typedef struct {
                                pysa_gb_tc_setup: 1 = tensor-core instance */
   int32_t plain_live;       /* host, from pysa_gb_tc_setup: bit v set when
                                plain variant v still has instances */
+  int32_t tc_fusable;       /* host, from pysa_gb_tc_setup: 1 when every
+                               tensor-core instance's R divides its chains
+                               per CTA (exchange can run inside the kernel) */
+  int32_t *tc_sched;        /* [2 + tc_num_items] device scratch of the
+                               persistent tensor-core kernel */
+  int32_t tc_unit_sweeps;   /* sweeps per work unit of that kernel (0: 4) */
   int32_t pad_;
 } pysa_gb_workspace;
 

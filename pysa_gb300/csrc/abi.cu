@@ -64,6 +64,23 @@ static int cuda_fail(cudaError_t e, const char* where) {
               std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// Most sweeps one fused tensor-core launch covers.
+constexpr int kMaxFusedSweeps = 32;
+
+// Streaming multiprocessors of the current device (cached per device).
+static int sm_count() {
+  static int cache[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 1;
+  if (cache[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 1;
+  }
+  return cache[dev];
+}
+
 // Per-device, per-variant launch geometry, filled on first use.
 struct VariantInfo {
   bool ready[2] = {false, false};
@@ -256,14 +273,14 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   if (items_n < 0) return items_n;
   if (!ws->tc_b || ws->tc_b_elems < need[0] || !ws->tc_diag ||
       ws->tc_diag_elems < need[1] || !ws->tc_items ||
-      ws->tc_num_items < items_n || !ws->tc_inst)
+      ws->tc_num_items < items_n || !ws->tc_inst || !ws->tc_sched)
     return fail(PYSA_GB_ERR_ARG, "tc workspace too small");
   cudaStream_t st = (cudaStream_t)stream;
   std::vector<int64_t> boff(p->num_instances), doff(p->num_instances);
   std::vector<int32_t> flags(p->num_instances, 0);
   const PlainItemPlan plan = make_item_plan();
   int64_t bo = 0, dd = 0;
-  int live = 0;
+  int live = 0, fusable = 1;
   for (int i = 0; i < p->num_instances; ++i) {
     boff[i] = bo;
     doff[i] = dd;
@@ -271,6 +288,7 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
       live |= 1 << plan.variant_of(host->n[i]);
       continue;
     }
+    if (tc_chains_per_cta(host->n[i]) % host->replicas[i] != 0) fusable = 0;
     flags[i] = 1;
     bo += tc_b_elems(host->n[i], ws->tc_terms);
     dd += tc_diag_elems(host->n[i]);
@@ -317,6 +335,7 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   }
   // host vectors above are pageable: the copies are complete on return
   ws->plain_live = live;
+  ws->tc_fusable = fusable;
   ws->tc_enabled = 1;
   return PYSA_GB_OK;
 }
@@ -403,18 +422,59 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.tc_diag = ws->tc_diag;
   ta.seed = o->seed;
   ta.recompute_every = o->recompute_every;
+  ta.use_pt = o->use_pt;
   ta.pad_ = 0;
+  ta.sched = ws->tc_sched;
   ta.trace = g_tc_trace;
+  const int sms = sm_count();
+  const int folds[3] = {1, 2, 4};
+  int last_v = -1;
+  for (int v = 0; v < 3; ++v)
+    if (ws->tc_variant_count[v] > 0) last_v = v;
+  // one persistent tensor-core launch per fold: `units` work units of
+  // `ku` sweeps per item, exchange fused or not
+  auto tc_launches = [&](int ku, int units, int fuse) -> int {
+    for (int v = 0; v < 3; ++v) {
+      const int count = ws->tc_variant_count[v];
+      if (count == 0) continue;
+      cudaError_t e = cudaMemsetAsync(ws->tc_sched, 0,
+                                      sizeof(int32_t) * (2 + (size_t)count), st);
+      if (e != cudaSuccess) return cuda_fail(e, "tc schedule reset");
+      ta.items = reinterpret_cast<const TcItem*>(ws->tc_items) +
+                 ws->tc_variant_start[v];
+      ta.num_items = count;
+      ta.unit_sweeps = ku;
+      ta.units_per_item = units;
+      ta.fuse_exchange = fuse;
+      ta.advance_counter = fuse && v == last_v;
+      e = launch_tc(ta, folds[v], sms, st);
+      if (e != cudaSuccess) return cuda_fail(e, "tc sweep launch");
+    }
+    return PYSA_GB_OK;
+  };
+  // Fused: every instance on the tensor cores, exchange inside the kernel
+  // (or none), no log-omega; several sweeps per launch with the fields
+  // resident in tensor memory.
+  const bool fused = use_tc && phases == 3 && ws->plain_live == 0 &&
+                     o->log_omega_stride == 0 &&
+                     (!o->use_pt || ws->tc_fusable) && ws->tc_sched;
+  if (fused) {
+    const int ku_pref = ws->tc_unit_sweeps > 0 ? ws->tc_unit_sweeps : 4;
+    int remaining = num_sweeps;
+    while (remaining > 0) {
+      int chunk = remaining < kMaxFusedSweeps ? remaining : kMaxFusedSweeps;
+      const int ku = chunk < ku_pref ? chunk : ku_pref;
+      chunk = chunk / ku * ku;
+      const int rc = tc_launches(ku, chunk / ku, 1);
+      if (rc != PYSA_GB_OK) return rc;
+      remaining -= chunk;
+    }
+    return PYSA_GB_OK;
+  }
   for (int sw = 0; sw < num_sweeps; ++sw) {
     if (use_tc && (phases & 1)) {
-      const int folds[3] = {1, 2, 4};
-      for (int v = 0; v < 3; ++v) {
-        if (ws->tc_variant_count[v] == 0) continue;
-        ta.items = reinterpret_cast<const TcItem*>(ws->tc_items) +
-                   ws->tc_variant_start[v];
-        cudaError_t e = launch_tc(ta, folds[v], ws->tc_variant_count[v], st);
-        if (e != cudaSuccess) return cuda_fail(e, "tc sweep launch");
-      }
+      const int rc = tc_launches(1, 1, 0);
+      if (rc != PYSA_GB_OK) return rc;
     }
     for (int v = 0; (phases & 1) && v < kNumPlainVariants; ++v) {
       if (v == 0 && random) launch_perm(pa, st);

@@ -114,6 +114,21 @@ __device__ __forceinline__ float log_uniform_f32(uint32_t x) {
   return __logf(__uint2float_rn(x) * 0x1p-32f + 0x1p-33f);
 }
 
+// Replica-exchange acceptance u < exp(de) (pysa/utils.py:50-55, oracle
+// form), with an f32 log-domain fast path that answers only outside its
+// error band.
+__device__ __forceinline__ bool pt_accept_lf(float de, float lf, uint32_t x) {
+  if (de >= 0.0f) return true;
+  if (de < -24.0f) return false;
+  const float margin = 3e-5f + 1e-6f * fabsf(de);
+  if (lf < de - margin) return true;
+  if (lf > de + margin) return false;
+  return uniform64(x) < exp((double)de);
+}
+__device__ __forceinline__ bool pt_accept(float de, uint32_t x) {
+  return pt_accept_lf(de, log_uniform_f32(x), x);
+}
+
 __device__ __forceinline__ bool metropolis_accept_lf(
     float dn, float beta, float lf, uint64_t seed, uint32_t inst,
     uint32_t sweep, uint32_t chain, uint32_t step) {

@@ -134,18 +134,6 @@ void launch_prepare(const PrepArgs& a, cudaStream_t st) {
 // counter.
 constexpr int kXWarps = 4;
 
-// Exchange acceptance u < exp(de) (oracle form), with an f32 log-domain fast
-// path that answers only outside its error band.
-__device__ __forceinline__ bool pt_accept(float de, uint32_t x) {
-  if (de >= 0.0f) return true;
-  if (de < -24.0f) return false;
-  const float uf = __uint2float_rn(x) * 0x1p-32f + 0x1p-33f;
-  const float lf = __logf(uf);
-  const float margin = 3e-5f + 1e-6f * fabsf(de);
-  if (lf < de - margin) return true;
-  if (lf > de + margin) return false;
-  return uniform64(x) < exp((double)de);
-}
 
 __global__ void k_exchange(const XArgs a) {
   __shared__ float E_s[kXWarps][kMaxReplicas];

@@ -57,7 +57,8 @@ struct TcCfg {
   // lf_full[2], lf_free[2], full[NS], free[NS]
   static constexpr int NBARS = 13 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
-  static constexpr size_t BYTES = MISC_OFF + 16;
+  // tmem slot, abort flag, current unit
+  static constexpr size_t BYTES = MISC_OFF + 24;
   static_assert(BYTES <= 232448, "shared memory budget");
 };
 
@@ -83,17 +84,15 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
   }
 }
 
-// Timeline stamp of CTA 0 when a trace buffer is given (diagnostics only).
-__device__ __forceinline__ void stamp(const TcArgs& a, int t, int slot) {
-  if (a.trace && blockIdx.x == 0) a.trace[t * 24 + slot] = globaltimer_ns();
+// Timeline stamps of CTA 0 when a trace buffer is given (diagnostics only):
+// row G < 48 per block, row 48 whole-unit marks (entry, set-up done, last
+// MMA done, fields stored, unit done, field load start; the last unit's).
+__device__ __forceinline__ void stamp(const TcArgs& a, uint32_t G, int slot) {
+  if (a.trace && blockIdx.x == 0 && G < 48)
+    a.trace[G * 24 + slot] = globaltimer_ns();
 }
-// Row t (= number of blocks) holds whole-CTA marks: slots 0-5 for CTA 0
-// (entry, set-up done, last MMA done, fields stored, exit, field load
-// start), slots 8-13 the same for the last CTA of the grid.
-__device__ __forceinline__ void stamp_cta(const TcArgs& a, int t, int slot) {
-  if (!a.trace) return;
-  if (blockIdx.x == 0) a.trace[t * 24 + slot] = globaltimer_ns();
-  if (blockIdx.x == gridDim.x - 1) a.trace[t * 24 + 8 + slot] = globaltimer_ns();
+__device__ __forceinline__ void stamp_cta(const TcArgs& a, int slot) {
+  if (a.trace && blockIdx.x == 0) a.trace[48 * 24 + slot] = globaltimer_ns();
 }
 
 // Named barriers in inline PTX: the warp is reconverged first and the
@@ -120,6 +119,12 @@ __device__ __forceinline__ uint32_t bf16_bits(float d) {
   return __float_as_uint(d) >> 16;
 }
 
+// Work units: unit u is item u % num_items for sweeps
+// sweep0 + (u / num_items) * unit_sweeps ... + unit_sweeps - 1.  CTAs take
+// units from a queue in order; a unit waits (bounded) until the same item's
+// previous unit is done, which a CTA that is already running owns, so the
+// wait always ends.  Within a unit the fields stay in TMEM across sweeps; the
+// replica exchange of the item's reads runs in the kernel when fused.
 template <int F>
 __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   using C = TcCfg<F>;
@@ -140,6 +145,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   sh.free_ = bars + 13 + C::NS;
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
+  volatile int32_t* unit_s =
+      reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 16);
   uint32_t* spins_s = reinterpret_cast<uint32_t*>(smem + C::SPIN_OFF);
   double* dE_s = reinterpret_cast<double*>(smem + C::DE_OFF);
   double* e0_s = reinterpret_cast<double*>(smem + C::E0_OFF);
@@ -149,32 +156,28 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
   float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
   float* corr_s = reinterpret_cast<float*>(smem + C::CORR_OFF);
+  // exchange scratch between sweeps (dl_s is idle then): energies [CC],
+  // per warp slot->replica, uniforms, their logs and the betas [4][CC] each
+  float* ex_E = dl_s;
+  int32_t* ex_B = reinterpret_cast<int32_t*>(dl_s + CC);
+  uint32_t* ex_X = reinterpret_cast<uint32_t*>(dl_s + 5 * CC);
+  float* ex_L = dl_s + 9 * CC;
+  float* ex_T = dl_s + 13 * CC;
   const uint32_t smem_base = smem_addr(smem);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int32_t* status = a.s.status;
-  const TcItem item = a.items[blockIdx.x];
-  const int inst = item.inst;
-  const int n = a.p.n[inst];
-  const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
-  const int S = NP / F;
-  const int NB = (n + 63) / 64;
-  const int NT = (S + 255) / 256;
-  const int T = a.terms;
-  const int words = (n + 31) >> 5;
   const bool ising = a.p.problem_type == PYSA_GB_ISING;
-  const uint32_t sweep = (uint32_t)(*a.s.sweep_counter);
-  const int64_t chain_base = a.p.chain_off[inst];
-  uint32_t ncols = 32;
-  while (ncols < (uint32_t)S) ncols <<= 1;
-  // recompute H = J s + h and E on the tensor cores at the start of this
-  // sweep (bounds the FP32 accumulator drift of the split-BF16 path)
-  const bool rc = a.recompute_every > 0 && (sweep % a.recompute_every) == 0;
+  const uint32_t sweep0 = (uint32_t)(*a.s.sweep_counter);
+  const int KU = a.unit_sweeps;
+  const int total_units = a.num_items * a.units_per_item;
+  const int T = a.terms;
+  constexpr uint32_t kCols = 512;
 
   // ---------------------------------------------------------------- set-up
-  if (threadIdx.x == 0) stamp_cta(a, NB, 0);
+  if (threadIdx.x == 0) stamp_cta(a, 0);
   if (warp == 0) {
-    tc::tmem_alloc(sh.tmem_slot, ncols);
+    tc::tmem_alloc(sh.tmem_slot, kCols);
     tc::tmem_relinquish();
   }
   if (threadIdx.x == 32) {
@@ -184,677 +187,817 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   }
   for (int i = threadIdx.x; i < (int)(C::A_BYTES / 16); i += blockDim.x)
     reinterpret_cast<uint4*>(smem + C::A_OFF)[i] = make_uint4(0, 0, 0, 0);
-  for (int i = threadIdx.x; i < CC * C::WORDS; i += blockDim.x) {
-    const int w = i / CC, c = i % CC;  // layout [word][chain]
-    spins_s[i] = (c < item.nchains && w < words)
-                     ? a.s.spins[(item.chain0 + c) * (int64_t)a.p.words + w]
-                     : 0u;
-  }
-  for (int c = threadIdx.x; c < CC; c += blockDim.x) {
-    dE_s[c] = 0.0;
-    e0_s[c] = c < item.nchains ? (double)a.s.energies[item.chain0 + c] : 0.0;
-    beta_s[c] = c < item.nchains ? a.s.chain_beta[item.chain0 + c] : 0.0f;
-  }
   fence_proxy_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *sh.tmem_slot;
+  const uint32_t idesc_full = tc::idesc_bf16(128, 256);
 
   // decision-thread identity: TMEM lane L = slice q, chain c
   const int L = threadIdx.x;
   const int q = L / CC, c = L % CC;
-  const bool valid = warp < 4 && c < item.nchains;
-  const int64_t chain = item.chain0 + c;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-
-  // Field rows move between HBM and TMEM through a per-warp shared-memory
-  // transpose (in the B ring, idle before the producer starts and after the
-  // last MMA): the warp reads 4 rows x 128 B per instruction, coalesced,
-  // then each thread takes its own row.
   float* stg = reinterpret_cast<float*>(smem + C::B_OFF) + warp * (32 * 33);
   const int w_c0 = (32 * warp) % CC, w_q = (32 * warp) / CC;
-  if (threadIdx.x == 0) stamp_cta(a, NB, 5);
-  if (warp < 4 && !rc) {  // local fields -> TMEM
-    // two 32-column chunks per round: 16 independent 16-byte loads in flight
-    auto load4 = [&](int j0, int it) {
-      const int col = w_q * S + j0 + 4 * (lane & 7);
-      const int cr = w_c0 + 4 * it + (lane >> 3);
-      float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (j0 < S && cr < item.nchains) {
-        const float* f =
-            a.fields + (item.chain0 + cr) * (int64_t)a.field_ld + col;
-        if (col + 4 <= n) {
-          v = *reinterpret_cast<const float4*>(f);
+
+  // per-role running counters (identical sequences in every role)
+  uint32_t G = 0;   // blocks
+  uint32_t RG = 0;  // recompute blocks
+  uint32_t u = 0;   // B ring stages (producer and MMA)
+
+  for (;;) {
+    // ------------------------------------------------------ next unit
+    if (threadIdx.x == 0) {
+      int un = -1;
+      if (!*sh.abort) {
+        un = (int)atomicAdd(reinterpret_cast<unsigned*>(a.sched), 1u);
+        if (un >= total_units) {
+          un = -1;
         } else {
-          v.x = col < n ? f[0] : 0.0f;
-          v.y = col + 1 < n ? f[1] : 0.0f;
-          v.z = col + 2 < n ? f[2] : 0.0f;
+          const int it = un % a.num_items, ch = un / a.num_items;
+          volatile int32_t* done = a.sched + 2 + it;
+          if (*done < ch) {
+            const uint64_t t0 = globaltimer_ns();
+            while (*done < ch) {
+              if (globaltimer_ns() - t0 > 1000000000ull) {
+                set_status(status, PYSA_GB_ERR_TIMEOUT);
+                *sh.abort = 1;
+                un = -1;
+                break;
+              }
+            }
+          }
+          __threadfence();  // the previous unit's stores are visible
         }
       }
-      return v;
+      *unit_s = un;
+    }
+    __syncthreads();
+    const int un = *unit_s;
+    if (un < 0) break;
+    const TcItem item = a.items[un % a.num_items];
+    const int chunk = un / a.num_items;
+    const uint32_t sweep_first = sweep0 + (uint32_t)(chunk * KU);
+    const int inst = item.inst;
+    const int n = a.p.n[inst];
+    const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
+    const int S = NP / F;
+    const int NB = (n + 63) / 64;
+    const int NT = (S + 255) / 256;
+    const int words = (n + 31) >> 5;
+    const int64_t chain_base = a.p.chain_off[inst];
+    const bool valid = warp < 4 && c < item.nchains;
+    const int64_t chain = item.chain0 + c;
+    const uint32_t chain_local = (uint32_t)(chain - chain_base);
+    const uint32_t G0 = G, RG0 = RG;
+    const uint32_t Gend = G0 + (uint32_t)(KU * NB);
+    auto rc_at = [&](int s) {
+      return a.recompute_every > 0 &&
+             ((sweep_first + (uint32_t)s) % (uint32_t)a.recompute_every) == 0;
     };
-    for (int j0 = 0; j0 < S; j0 += 64) {
-      float4 va[8], vb[8];
-#pragma unroll
-      for (int it = 0; it < 8; ++it) {
-        va[it] = load4(j0, it);
-        vb[it] = load4(j0 + 32, it);
-      }
-#pragma unroll
-      for (int h2 = 0; h2 < 2; ++h2) {
-        if (j0 + 32 * h2 >= S) break;
-#pragma unroll
-        for (int it = 0; it < 8; ++it) {
-          const float4 v = h2 ? vb[it] : va[it];
-          float* d = stg + (4 * it + (lane >> 3)) * 33 + 4 * (lane & 7);
-          d[0] = v.x;
-          d[1] = v.y;
-          d[2] = v.z;
-          d[3] = v.w;
-        }
-        __syncwarp();
-        float v[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = stg[lane * 33 + i];
-        __syncwarp();
-        tc::tmem_st32(taddr + lane_base + j0 + 32 * h2, v);
-      }
-    }
-    tc::tmem_wait_st();
-    fence_proxy_async();
-    tc::fence_before_sync();
-  }
-  __syncthreads();
-  tc::fence_after_sync();
-  if (threadIdx.x == 0) stamp_cta(a, NB, 1);
+    int n_rc = 0;
+    for (int s = 0; s < KU; ++s) n_rc += rc_at(s) ? 1 : 0;
 
-  const uint32_t idesc_full = tc::idesc_bf16(128, 256);
-
-  if (warp < 4 && rc) {
-    // ================================================ recompute: A = spins
-    for (int t = 0; t < NB; ++t) {
-      bool go = q == 0 && !*sh.abort;
-      if (go && t > 0) go = tc_wait(sh.rc_done, (t - 1) & 1, sh, status);
-      go = __all_sync(0xffffffffu, go);
-      if (go) {
-        const uint32_t w0 = spins_s[(2 * t) * CC + c];
-        const uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
-        const int kmax = n - 64 * t < 64 ? n - 64 * t : 64;
-        uint32_t pk[32];
-#pragma unroll
-        for (int k = 0; k < 64; ++k) {
-          const bool sb = k < 32 ? ((w0 >> k) & 1u) : ((w1 >> (k - 32)) & 1u);
-          const float v = (!valid || k >= kmax) ? 0.0f
-                          : sb ? 1.0f : (ising ? -1.0f : 0.0f);
-          const uint32_t b16 = bf16_bits(v);
-          if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
-        }
-#pragma unroll
-        for (int qq = 0; qq < F; ++qq) {
-          const int m = qq * CC + c;
-          unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                ((m >> 3) * 8) * 128 + (m & 7) * 16;
-#pragma unroll
-          for (int kc = 0; kc < 8; ++kc)
-            *reinterpret_cast<uint4*>(rowp + kc * 128) =
-                make_uint4(pk[4 * kc], pk[4 * kc + 1], pk[4 * kc + 2],
-                           pk[4 * kc + 3]);
-        }
-        fence_proxy_async();
-      }
-      named_sync_128();
-      if (threadIdx.x == 0) mbar_arrive(sh.rc_full);
+    // ------------------------------------------------ unit prologue
+    for (int i = threadIdx.x; i < CC * C::WORDS; i += blockDim.x) {
+      const int w = i / CC, cc = i % CC;  // layout [word][chain]
+      spins_s[i] = (cc < item.nchains && w < words)
+                       ? __ldcg(a.s.spins + (item.chain0 + cc) * (int64_t)a.p.words + w)
+                       : 0u;
     }
-    if (!*sh.abort && NB > 0) tc_wait(sh.rc_done, (NB - 1) & 1, sh, status);
-    tc::fence_after_sync();
-    // H = J s + h in TMEM; partial energies sum_j s_j ((J s)_j / 2 + h_j)
-    const float* hh = a.p.h + a.p.h_off[inst];
-    double ep = 0.0;
-    if (__all_sync(0xffffffffu, !*sh.abort)) {
-      for (int j0 = 0; j0 < S; j0 += 32) {
-        float v[32];
-        tc::tmem_ld32(taddr + lane_base + j0, v);
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int col = q * S + j0 + i;
-          if (col < n) {
-            const uint32_t wv = spins_s[(col >> 5) * CC + c];
-            const double sj =
-                ((wv >> (col & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
-            const float hj = hh[col];
-            ep += sj * (0.5 * (double)v[i] + (double)hj);
-            v[i] = v[i] + hj;
+    for (int cc = threadIdx.x; cc < CC; cc += blockDim.x) {
+      dE_s[cc] = 0.0;
+      // state written by other CTAs of this launch: loads bypass L1
+      e0_s[cc] = cc < item.nchains
+                     ? (double)__ldcg(a.s.energies + item.chain0 + cc)
+                     : 0.0;
+      beta_s[cc] =
+          cc < item.nchains ? __ldcg(a.s.chain_beta + item.chain0 + cc) : 0.0f;
+    }
+    if (threadIdx.x == 0) stamp_cta(a, 5);
+    if (warp < 4 && !rc_at(0)) {  // local fields -> TMEM
+      // two 32-column chunks per round: 16 independent 16-byte loads in
+      // flight; rows move through a per-warp shared-memory transpose (in
+      // the B ring, idle until the producer starts)
+      auto load4 = [&](int j0, int it) {
+        const int col = w_q * S + j0 + 4 * (lane & 7);
+        const int cr = w_c0 + 4 * it + (lane >> 3);
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (j0 < S && cr < item.nchains) {
+          const float* f =
+              a.fields + (item.chain0 + cr) * (int64_t)a.field_ld + col;
+          if (col + 4 <= n) {
+            v = __ldcg(reinterpret_cast<const float4*>(f));
+          } else {
+            v.x = col < n ? __ldcg(f) : 0.0f;
+            v.y = col + 1 < n ? __ldcg(f + 1) : 0.0f;
+            v.z = col + 2 < n ? __ldcg(f + 2) : 0.0f;
           }
         }
-        tc::tmem_st32(taddr + lane_base + j0, v);
+        return v;
+      };
+      for (int j0 = 0; j0 < S; j0 += 64) {
+        float4 va[8], vb[8];
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+          va[it] = load4(j0, it);
+          vb[it] = load4(j0 + 32, it);
+        }
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+#pragma unroll
+          for (int it = 0; it < 8; ++it) {
+            const float4 v = h2 ? vb[it] : va[it];
+            float* d = stg + (4 * it + (lane >> 3)) * 33 + 4 * (lane & 7);
+            d[0] = v.x;
+            d[1] = v.y;
+            d[2] = v.z;
+            d[3] = v.w;
+          }
+          __syncwarp();
+          float v[32];
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = stg[lane * 33 + i];
+          __syncwarp();
+          tc::tmem_st32(taddr + lane_base + j0 + 32 * h2, v);
+        }
       }
       tc::tmem_wait_st();
     }
-    epart_s[q * CC + c] = ep;
+    fence_proxy_async();
     tc::fence_before_sync();
-    named_sync_128();
+    __syncthreads();
     tc::fence_after_sync();
-    if (q == 0 && valid) {
-      double e = 0.0;
-      for (int qq = 0; qq < F; ++qq) e += epart_s[qq * CC + c];
-      e0_s[c] = (double)(float)e;
-    }
-    named_sync_128();
-  }
+    if (threadIdx.x == 0) stamp_cta(a, 1);
 
-  if (warp < 4) {
-    // ============================================================ decide
-    const uint32_t chain_local = (uint32_t)(chain - chain_base);
-    const float beta = beta_s[c];
-    // every decision thread runs all NB iterations (named barrier inside);
-    // after an abort the work is skipped
-    for (int t = 0; t < NB; ++t) {
-      const int i0 = 64 * t;
-      const int qt = i0 / S, co = i0 % S;
-      const int kmax = n - i0 < 64 ? n - i0 : 64;
-      bool go = q == qt && !*sh.abort;
-      if (go && t > 0) go = tc_wait(sh.h_ready, (t - 1) & 1, sh, status);
-      if (go) go = tc_wait(&sh.jbb_full[t & 1], (t >> 1) & 1, sh, status);
-      if (go) go = tc_wait(&sh.lf_full[t & 1], (t >> 1) & 1, sh, status);
-      // warp-uniform, so the warp-collective TMEM loads below stay converged
-      go = __all_sync(0xffffffffu, go);
-      const bool lead = go && c == 0;
-      if (lead) stamp(a, t, 0);
-      if (go) {
-        tc::fence_after_sync();
-        if (lead) stamp(a, t, 1);
-        const float* jb = jbb + (t & 1) * 4096;
-        const float* lfb = lf_s + (t & 1) * 64 * CC;
-        const uint32_t o0 = spins_s[(2 * t) * CC + c];
-        const uint32_t o1 = spins_s[(2 * t + 1) * CC + c];
-        uint32_t w0 = o0, w1 = o1;
-        float dEb = 0.0f;
-        bool a_ok = true;
-        // four sub-blocks of 16 spins; corrections from earlier sub-blocks
-        // are applied lazily when a sub-block's fields are loaded
-#pragma unroll 1
-        for (int g = 0; g < 4; ++g) {
-          float hs[16];
-          tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
-          if (lead) stamp(a, t, 8 + 3 * g);
-          // with helpers, sub-blocks older than g-1 arrive precomputed
-          const int k_lo = (C::HELP && g >= 2) ? 16 * (g - 1) : 0;
-          if (C::HELP && g >= 2) {
+    if (warp < 4) {
+      for (int s = 0; s < KU; ++s) {
+        const uint32_t sweep = sweep_first + (uint32_t)s;
+        const uint32_t Gs = G0 + (uint32_t)(s * NB);  // first block of sweep
+        if (rc_at(s)) {
+          // ========================================== recompute: A = spins
+          // the previous sweep's MMAs (which read A) must be done
+          bool rok = true;
+          if (s > 0) rok = tc_wait(sh.mma_done, (Gs - 1) & 1, sh, status);
+          for (int t = 0; t < NB; ++t) {
+            const uint32_t R_ = RG + (uint32_t)t;
+            bool go = rok && q == 0 && !*sh.abort;
+            if (go && t > 0) go = tc_wait(sh.rc_done, (R_ - 1) & 1, sh, status);
+            go = __all_sync(0xffffffffu, go);
+            if (go) {
+              const uint32_t w0 = spins_s[(2 * t) * CC + c];
+              const uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
+              const int kmax = n - 64 * t < 64 ? n - 64 * t : 64;
+              uint32_t pk[32];
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-              hs[j] += corr_s[((g - 2) * 16 + j) * CC + c];
-          }
-#pragma unroll 2
-          for (int k = k_lo; k < 16 * g; ++k) {
-            const float d = dl_s[k * CC + c];
-            const float4* jr =
-                reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
-#pragma unroll
-            for (int q4 = 0; q4 < 4; ++q4) {
-              const float4 v = jr[q4];
-              hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
-              hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
-              hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
-              hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
-            }
-          }
-          if (lead) stamp(a, t, 9 + 3 * g);
-          uint32_t wcur = g < 2 ? w0 : w1;
-          const int sb = 16 * (g & 1);
-          // fast pass: branch-free decisions from the precomputed log-uniform;
-          // a decision inside the f32 error band is only flagged here
-          const uint32_t wsave = wcur;
-          const float dEsave = dEb;
-          float hsave[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) hsave[j] = hs[j];
-          bool unc = false;
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int k = 16 * g + j;
-            const bool sbit = (wcur >> (sb + j)) & 1u;
-            const float hk = hs[j];
-            const float dn =
-                ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
-            const float lfk = lfb[k * CC + c];
-            const float bd = beta * dn;
-            const float margin = 3e-5f + 1e-6f * fabsf(bd);
-            const bool live = valid && k < kmax;
-            const bool yes = dn >= 0.0f || lfk < bd - margin;
-            const bool no = bd < -24.0f || lfk > bd + margin;
-            unc |= live && !yes && !no;
-            const bool acc = live && yes;
-            const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
-                                          : (sbit ? -1.0f : 1.0f))
-                                 : 0.0f;
-            dl_s[k * CC + c] = dl;
-            dEb = acc ? dEb - dn : dEb;
-            wcur ^= acc ? (1u << (sb + j)) : 0u;
-            if (j < 15) {  // exact corrections inside the sub-block
-              const float4* jr =
-                  reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
-#pragma unroll
-              for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
-                const float4 v = jr[q4];
-                if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
-                if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
-                if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
-                if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+              for (int k = 0; k < 64; ++k) {
+                const bool sb =
+                    k < 32 ? ((w0 >> k) & 1u) : ((w1 >> (k - 32)) & 1u);
+                const float v = (!valid || k >= kmax) ? 0.0f
+                                : sb ? 1.0f : (ising ? -1.0f : 0.0f);
+                const uint32_t b16 = bf16_bits(v);
+                if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
               }
-            }
-          }
-          if (__any_sync(0xffffffffu, unc)) {
-            // rare: redo the sub-block with the exact f64 rule where needed
-            wcur = wsave;
-            dEb = dEsave;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) hs[j] = hsave[j];
+              for (int qq = 0; qq < F; ++qq) {
+                const int m = qq * CC + c;
+                unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                      ((m >> 3) * 8) * 128 + (m & 7) * 16;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int k = 16 * g + j;
-              const bool sbit = (wcur >> (sb + j)) & 1u;
-              const float hk = hs[j];
-              const float dn =
-                  ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
-              const bool acc =
-                  valid && k < kmax &&
-                  metropolis_accept_lf(dn, beta, lfb[k * CC + c], a.seed,
-                                       (uint32_t)inst, sweep, chain_local,
-                                       (uint32_t)(i0 + k));
-              const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
-                                            : (sbit ? -1.0f : 1.0f))
-                                   : 0.0f;
-              dl_s[k * CC + c] = dl;
-              if (acc) {
-                dEb -= dn;
-                wcur ^= 1u << (sb + j);
+                for (int kc = 0; kc < 8; ++kc)
+                  *reinterpret_cast<uint4*>(rowp + kc * 128) =
+                      make_uint4(pk[4 * kc], pk[4 * kc + 1], pk[4 * kc + 2],
+                                 pk[4 * kc + 3]);
               }
-              if (j < 15) {
+              fence_proxy_async();
+            }
+            named_sync_128();
+            if (threadIdx.x == 0) mbar_arrive(sh.rc_full);
+          }
+          if (!*sh.abort && NB > 0)
+            tc_wait(sh.rc_done, (RG + NB - 1) & 1, sh, status);
+          RG += NB;
+          tc::fence_after_sync();
+          // H = J s + h in TMEM; energies sum_j s_j ((J s)_j / 2 + h_j)
+          const float* hh = a.p.h + a.p.h_off[inst];
+          double ep = 0.0;
+          if (__all_sync(0xffffffffu, !*sh.abort)) {
+            for (int j0 = 0; j0 < S; j0 += 32) {
+              float v[32];
+              tc::tmem_ld32(taddr + lane_base + j0, v);
+#pragma unroll
+              for (int i = 0; i < 32; ++i) {
+                const int col = q * S + j0 + i;
+                if (col < n) {
+                  const uint32_t wv = spins_s[(col >> 5) * CC + c];
+                  const double sj =
+                      ((wv >> (col & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+                  const float hj = hh[col];
+                  ep += sj * (0.5 * (double)v[i] + (double)hj);
+                  v[i] = v[i] + hj;
+                }
+              }
+              tc::tmem_st32(taddr + lane_base + j0, v);
+            }
+            tc::tmem_wait_st();
+          }
+          epart_s[q * CC + c] = ep;
+          tc::fence_before_sync();
+          named_sync_128();
+          tc::fence_after_sync();
+          if (q == 0 && valid) {
+            double e = 0.0;
+            for (int qq = 0; qq < F; ++qq) e += epart_s[qq * CC + c];
+            e0_s[c] = (double)(float)e;
+            dE_s[c] = 0.0;
+          }
+          named_sync_128();
+        }
+
+        // ============================================================ decide
+        const float beta = beta_s[c];
+        for (int t = 0; t < NB; ++t) {
+          const uint32_t Gb = Gs + (uint32_t)t;
+          const int i0 = 64 * t;
+          const int qt = i0 / S, co = i0 % S;
+          const int kmax = n - i0 < 64 ? n - i0 : 64;
+          bool go = q == qt && !*sh.abort;
+          // fields of this block: the previous block's critical MMA (not
+          // needed for a unit's first block or after a recompute)
+          if (go && Gb > G0 && !(t == 0 && rc_at(s)))
+            go = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
+          if (go) go = tc_wait(&sh.jbb_full[Gb & 1], (Gb >> 1) & 1, sh, status);
+          if (go) go = tc_wait(&sh.lf_full[Gb & 1], (Gb >> 1) & 1, sh, status);
+          // warp-uniform, so the warp-collective TMEM loads below stay
+          // converged
+          go = __all_sync(0xffffffffu, go);
+          const bool lead = go && c == 0;
+          if (lead) stamp(a, Gb, 0);
+          if (go) {
+            tc::fence_after_sync();
+            if (lead) stamp(a, Gb, 1);
+            const float* jb = jbb + (Gb & 1) * 4096;
+            const float* lfb = lf_s + (Gb & 1) * 64 * CC;
+            const uint32_t o0 = spins_s[(2 * t) * CC + c];
+            const uint32_t o1 = spins_s[(2 * t + 1) * CC + c];
+            uint32_t w0 = o0, w1 = o1;
+            float dEb = 0.0f;
+            bool a_ok = true;
+            // four sub-blocks of 16 spins; corrections from earlier sub-blocks
+            // are applied lazily when a sub-block's fields are loaded
+    #pragma unroll 1
+            for (int g = 0; g < 4; ++g) {
+              float hs[16];
+              tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
+              if (lead) stamp(a, Gb, 8 + 3 * g);
+              // with helpers, sub-blocks older than g-1 arrive precomputed
+              const int k_lo = (C::HELP && g >= 2) ? 16 * (g - 1) : 0;
+              if (C::HELP && g >= 2) {
+    #pragma unroll
+                for (int j = 0; j < 16; ++j)
+                  hs[j] += corr_s[((g - 2) * 16 + j) * CC + c];
+              }
+    #pragma unroll 2
+              for (int k = k_lo; k < 16 * g; ++k) {
+                const float d = dl_s[k * CC + c];
                 const float4* jr =
                     reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
-#pragma unroll
-                for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
+    #pragma unroll
+                for (int q4 = 0; q4 < 4; ++q4) {
                   const float4 v = jr[q4];
-                  if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
-                  if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
-                  if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
-                  if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+                  hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
+                  hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
+                  hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
+                  hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
+                }
+              }
+              if (lead) stamp(a, Gb, 9 + 3 * g);
+              uint32_t wcur = g < 2 ? w0 : w1;
+              const int sb = 16 * (g & 1);
+              // fast pass: branch-free decisions from the precomputed log-uniform;
+              // a decision inside the f32 error band is only flagged here
+              const uint32_t wsave = wcur;
+              const float dEsave = dEb;
+              float hsave[16];
+    #pragma unroll
+              for (int j = 0; j < 16; ++j) hsave[j] = hs[j];
+              bool unc = false;
+    #pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int k = 16 * g + j;
+                const bool sbit = (wcur >> (sb + j)) & 1u;
+                const float hk = hs[j];
+                const float dn =
+                    ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
+                const float lfk = lfb[k * CC + c];
+                const float bd = beta * dn;
+                const float margin = 3e-5f + 1e-6f * fabsf(bd);
+                const bool live = valid && k < kmax;
+                const bool yes = dn >= 0.0f || lfk < bd - margin;
+                const bool no = bd < -24.0f || lfk > bd + margin;
+                unc |= live && !yes && !no;
+                const bool acc = live && yes;
+                const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
+                                              : (sbit ? -1.0f : 1.0f))
+                                     : 0.0f;
+                dl_s[k * CC + c] = dl;
+                dEb = acc ? dEb - dn : dEb;
+                wcur ^= acc ? (1u << (sb + j)) : 0u;
+                if (j < 15) {  // exact corrections inside the sub-block
+                  const float4* jr =
+                      reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
+    #pragma unroll
+                  for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
+                    const float4 v = jr[q4];
+                    if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
+                    if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
+                    if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
+                    if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+                  }
+                }
+              }
+              if (__any_sync(0xffffffffu, unc)) {
+                // rare: redo the sub-block with the exact f64 rule where needed
+                wcur = wsave;
+                dEb = dEsave;
+    #pragma unroll
+                for (int j = 0; j < 16; ++j) hs[j] = hsave[j];
+    #pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  const int k = 16 * g + j;
+                  const bool sbit = (wcur >> (sb + j)) & 1u;
+                  const float hk = hs[j];
+                  const float dn =
+                      ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
+                  const bool acc =
+                      valid && k < kmax &&
+                      metropolis_accept_lf(dn, beta, lfb[k * CC + c], a.seed,
+                                           (uint32_t)inst, sweep, chain_local,
+                                           (uint32_t)(i0 + k));
+                  const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
+                                                : (sbit ? -1.0f : 1.0f))
+                                       : 0.0f;
+                  dl_s[k * CC + c] = dl;
+                  if (acc) {
+                    dEb -= dn;
+                    wcur ^= 1u << (sb + j);
+                  }
+                  if (j < 15) {
+                    const float4* jr =
+                        reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
+    #pragma unroll
+                    for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
+                      const float4 v = jr[q4];
+                      if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
+                      if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
+                      if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
+                      if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+                    }
+                  }
+                }
+              }
+              if (g < 2) w0 = wcur; else w1 = wcur;
+              if (lead) stamp(a, Gb, 10 + 3 * g);
+              if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
+            }
+            // the block's deltas (kept in dl_s) into the A rows; A is
+            // single-buffered, so the previous block's MMAs must be done (they
+            // normally finished while this block was being decided)
+            if (Gb > G0) {
+              if (lead) stamp(a, Gb, 2);
+              a_ok = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
+              if (lead) stamp(a, Gb, 3);
+            }
+            if (a_ok) {
+    #pragma unroll 1
+              for (int g = 0; g < 4; ++g) {
+                uint32_t pkg[8];
+    #pragma unroll
+                for (int j = 0; j < 16; j += 2)
+                  pkg[j >> 1] = bf16_bits(dl_s[(16 * g + j) * CC + c]) |
+                                (bf16_bits(dl_s[(16 * g + j + 1) * CC + c]) << 16);
+    #pragma unroll
+                for (int qq = 0; qq < F; ++qq) {
+                  const int m = qq * CC + c;
+                  unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                        ((m >> 3) * 8) * 128 + (m & 7) * 16;
+                  *reinterpret_cast<uint4*>(rowp + (2 * g) * 128) =
+                      make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+                  *reinterpret_cast<uint4*>(rowp + (2 * g + 1) * 128) =
+                      make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
                 }
               }
             }
+            if (valid) {
+              spins_s[(2 * t) * CC + c] = w0;
+              spins_s[(2 * t + 1) * CC + c] = w1;
+              dE_s[c] += (double)dEb;
+            }
+            fence_proxy_async();
+          } else if (C::HELP) {
+            // helper (the other slice's thread of chain c), or a deciding
+            // thread after an abort: same three barriers as the deciding path
+            const bool hgo = __all_sync(0xffffffffu, !*sh.abort) && q != qt;
+            const float* jb = jbb + (Gb & 1) * 4096;
+            float c3[16];
+    #pragma unroll
+            for (int j = 0; j < 16; ++j) c3[j] = 0.0f;
+            named_sync_dec();  // sub-block 0 decided
+            bool hok = hgo && valid &&
+                       tc_wait(&sh.jbb_full[Gb & 1], (Gb >> 1) & 1, sh, status);
+            if (hok) {
+              float c2[16];
+    #pragma unroll
+              for (int j = 0; j < 16; ++j) c2[j] = 0.0f;
+    #pragma unroll 2
+              for (int k = 0; k < 16; ++k) {
+                const float d = dl_s[k * CC + c];
+                const float4* jr = reinterpret_cast<const float4*>(jb + k * 64);
+    #pragma unroll
+                for (int q4 = 0; q4 < 4; ++q4) {
+                  const float4 v2 = jr[8 + q4], v3 = jr[12 + q4];
+                  c2[4 * q4 + 0] = fmaf(d, v2.x, c2[4 * q4 + 0]);
+                  c2[4 * q4 + 1] = fmaf(d, v2.y, c2[4 * q4 + 1]);
+                  c2[4 * q4 + 2] = fmaf(d, v2.z, c2[4 * q4 + 2]);
+                  c2[4 * q4 + 3] = fmaf(d, v2.w, c2[4 * q4 + 3]);
+                  c3[4 * q4 + 0] = fmaf(d, v3.x, c3[4 * q4 + 0]);
+                  c3[4 * q4 + 1] = fmaf(d, v3.y, c3[4 * q4 + 1]);
+                  c3[4 * q4 + 2] = fmaf(d, v3.z, c3[4 * q4 + 2]);
+                  c3[4 * q4 + 3] = fmaf(d, v3.w, c3[4 * q4 + 3]);
+                }
+              }
+    #pragma unroll
+              for (int j = 0; j < 16; ++j) corr_s[j * CC + c] = c2[j];
+            }
+            named_sync_dec();  // sub-block 1 decided; corrections of 2 out
+            if (hok) {
+    #pragma unroll 2
+              for (int k = 16; k < 32; ++k) {
+                const float d = dl_s[k * CC + c];
+                const float4* jr = reinterpret_cast<const float4*>(jb + k * 64);
+    #pragma unroll
+                for (int q4 = 0; q4 < 4; ++q4) {
+                  const float4 v3 = jr[12 + q4];
+                  c3[4 * q4 + 0] = fmaf(d, v3.x, c3[4 * q4 + 0]);
+                  c3[4 * q4 + 1] = fmaf(d, v3.y, c3[4 * q4 + 1]);
+                  c3[4 * q4 + 2] = fmaf(d, v3.z, c3[4 * q4 + 2]);
+                  c3[4 * q4 + 3] = fmaf(d, v3.w, c3[4 * q4 + 3]);
+                }
+              }
+    #pragma unroll
+              for (int j = 0; j < 16; ++j) corr_s[(16 + j) * CC + c] = c3[j];
+            }
+            named_sync_dec();  // sub-block 2 decided; corrections of 3 out
           }
-          if (g < 2) w0 = wcur; else w1 = wcur;
-          if (lead) stamp(a, t, 10 + 3 * g);
-          if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
+          if (lane == 0) stamp(a, Gb, 20 + warp);
+          named_sync_128();
+          if (threadIdx.x == 0) {
+            stamp(a, Gb, 4);
+            mbar_arrive(sh.a_full);
+            mbar_arrive(&sh.jbb_free[Gb & 1]);
+            mbar_arrive(&sh.lf_free[Gb & 1]);
+          }
+        }  // blocks
+
+        // ------------------------------------------------ end of the sweep
+        // energy of the sweep's last state, per-chain best (strict <,
+        // pysa/simulation.py:150-171), then the exchange of the item's reads
+        if (q == 0 && valid && !*sh.abort) {
+          const float e_f = (float)(e0_s[c] + dE_s[c]);
+          if (e_f < __ldcg(a.s.best_energy + chain)) {
+            a.s.best_energy[chain] = e_f;
+            a.s.best_sweep[chain] = (int32_t)sweep;
+            for (int w = 0; w < words; ++w)
+              a.s.best_spins[chain * a.p.words + w] = spins_s[w * CC + c];
+          }
+          e0_s[c] = (double)e_f;
+          dE_s[c] = 0.0;
+          ex_E[c] = e_f;
         }
-        // the block's deltas (kept in dl_s) into the A rows; A is
-        // single-buffered, so the previous block's MMAs must be done (they
-        // normally finished while this block was being decided)
-        if (t > 0) {
-          if (lead) stamp(a, t, 2);
-          a_ok = tc_wait(sh.mma_done, (t - 1) & 1, sh, status);
-          if (lead) stamp(a, t, 3);
+        named_sync_128();
+        if (a.fuse_exchange && a.use_pt && !*sh.abort) {
+          // pysa/utils.py:44-58 per read, warp per read: pairs (R-1, R-2),
+          // (R-2, R-3), ... in order; uniforms of stream (PT, inst, sweep,
+          // read, pair)
+          const int R = a.p.replicas[inst];
+          const float* betas = a.p.ladder + a.p.ladder_off[inst];
+          const int nreads = item.nchains / R;
+          int32_t* B = ex_B + warp * CC;
+          uint32_t* X = ex_X + warp * CC;
+          float* Lx = ex_L + warp * CC;
+          float* Bt = ex_T + warp * CC;
+          for (int k = lane; k < R; k += 32) Bt[k] = betas[k];
+          for (int r = warp; r < nreads; r += 4) {
+            const int64_t gbase = item.chain0 + (int64_t)r * R;
+            const uint32_t lread = (uint32_t)((gbase - chain_base) / R);
+            const float* E = ex_E + r * R;
+            for (int k = lane; k < R; k += 32) {
+              B[k] = __ldcg(a.s.beta_idx + gbase + k);
+              if (k < R - 1) {
+                const uint32_t x = draw1(a.seed, TAG_PT, (uint32_t)inst, sweep,
+                                         lread, (uint32_t)k);
+                X[k] = x;
+                Lx[k] = log_uniform_f32(x);
+              }
+            }
+            __syncwarp();
+            if (lane == 0) {
+              for (int k = 0; k < R - 1; ++k) {
+                const int k1 = R - k - 1, k2 = R - k - 2;
+                const int b1 = B[k1], b2 = B[k2];
+                const float de = __fmul_rn(__fsub_rn(E[b1], E[b2]),
+                                           __fsub_rn(Bt[k1], Bt[k2]));
+                if (pt_accept_lf(de, Lx[k], X[k])) {
+                  B[k1] = b2;
+                  B[k2] = b1;
+                }
+              }
+            }
+            __syncwarp();
+            for (int k = lane; k < R; k += 32) {
+              a.s.beta_idx[gbase + k] = B[k];
+              a.s.chain_beta[gbase + B[k]] = Bt[k];
+              beta_s[r * R + B[k]] = Bt[k];
+            }
+            __syncwarp();
+          }
         }
-        if (a_ok) {
-#pragma unroll 1
-          for (int g = 0; g < 4; ++g) {
-            uint32_t pkg[8];
+        named_sync_128();
+      }  // sweeps
+
+      // ----------------------------------------------------------- epilogue
+      if (!*sh.abort) tc_wait(sh.mma_done, (Gend - 1) & 1, sh, status);
+      tc::fence_after_sync();
+      if (threadIdx.x == 0) stamp_cta(a, 2);
+      if (__all_sync(0xffffffffu, !*sh.abort)) {
+        for (int j0 = 0; j0 < S; j0 += 32) {
+          float v[32];
+          tc::tmem_ld32(taddr + lane_base + j0, v);
 #pragma unroll
-            for (int j = 0; j < 16; j += 2)
-              pkg[j >> 1] = bf16_bits(dl_s[(16 * g + j) * CC + c]) |
-                            (bf16_bits(dl_s[(16 * g + j + 1) * CC + c]) << 16);
+          for (int i = 0; i < 32; ++i) stg[lane * 33 + i] = v[i];
+          __syncwarp();
+          const int col = w_q * S + j0 + 4 * (lane & 7);
 #pragma unroll
-            for (int qq = 0; qq < F; ++qq) {
-              const int m = qq * CC + c;
-              unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                    ((m >> 3) * 8) * 128 + (m & 7) * 16;
-              *reinterpret_cast<uint4*>(rowp + (2 * g) * 128) =
-                  make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
-              *reinterpret_cast<uint4*>(rowp + (2 * g + 1) * 128) =
-                  make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
+          for (int it = 0; it < 8; ++it) {
+            const int rr = 4 * it + (lane >> 3);
+            const int cr = w_c0 + rr;
+            if (cr < item.nchains && col < n) {
+              const float* sv = stg + rr * 33 + 4 * (lane & 7);
+              float* f =
+                  a.fields + (item.chain0 + cr) * (int64_t)a.field_ld + col;
+              if (col + 4 <= n) {
+                *reinterpret_cast<float4*>(f) =
+                    make_float4(sv[0], sv[1], sv[2], sv[3]);
+              } else {
+                f[0] = sv[0];
+                if (col + 1 < n) f[1] = sv[1];
+                if (col + 2 < n) f[2] = sv[2];
+              }
             }
           }
+          __syncwarp();
         }
-        if (valid) {
-          spins_s[(2 * t) * CC + c] = w0;
-          spins_s[(2 * t + 1) * CC + c] = w1;
-          dE_s[c] += (double)dEb;
-        }
-        fence_proxy_async();
-      } else if (C::HELP) {
-        // helper (the other slice's thread of chain c), or a deciding
-        // thread after an abort: same three barriers as the deciding path
-        const bool hgo = __all_sync(0xffffffffu, !*sh.abort) && q != qt;
-        const float* jb = jbb + (t & 1) * 4096;
-        float c3[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) c3[j] = 0.0f;
-        named_sync_dec();  // sub-block 0 decided
-        bool hok = hgo && valid &&
-                   tc_wait(&sh.jbb_full[t & 1], (t >> 1) & 1, sh, status);
-        if (hok) {
-          float c2[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) c2[j] = 0.0f;
-#pragma unroll 2
-          for (int k = 0; k < 16; ++k) {
-            const float d = dl_s[k * CC + c];
-            const float4* jr = reinterpret_cast<const float4*>(jb + k * 64);
-#pragma unroll
-            for (int q4 = 0; q4 < 4; ++q4) {
-              const float4 v2 = jr[8 + q4], v3 = jr[12 + q4];
-              c2[4 * q4 + 0] = fmaf(d, v2.x, c2[4 * q4 + 0]);
-              c2[4 * q4 + 1] = fmaf(d, v2.y, c2[4 * q4 + 1]);
-              c2[4 * q4 + 2] = fmaf(d, v2.z, c2[4 * q4 + 2]);
-              c2[4 * q4 + 3] = fmaf(d, v2.w, c2[4 * q4 + 3]);
-              c3[4 * q4 + 0] = fmaf(d, v3.x, c3[4 * q4 + 0]);
-              c3[4 * q4 + 1] = fmaf(d, v3.y, c3[4 * q4 + 1]);
-              c3[4 * q4 + 2] = fmaf(d, v3.z, c3[4 * q4 + 2]);
-              c3[4 * q4 + 3] = fmaf(d, v3.w, c3[4 * q4 + 3]);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) corr_s[j * CC + c] = c2[j];
-        }
-        named_sync_dec();  // sub-block 1 decided; corrections of 2 out
-        if (hok) {
-#pragma unroll 2
-          for (int k = 16; k < 32; ++k) {
-            const float d = dl_s[k * CC + c];
-            const float4* jr = reinterpret_cast<const float4*>(jb + k * 64);
-#pragma unroll
-            for (int q4 = 0; q4 < 4; ++q4) {
-              const float4 v3 = jr[12 + q4];
-              c3[4 * q4 + 0] = fmaf(d, v3.x, c3[4 * q4 + 0]);
-              c3[4 * q4 + 1] = fmaf(d, v3.y, c3[4 * q4 + 1]);
-              c3[4 * q4 + 2] = fmaf(d, v3.z, c3[4 * q4 + 2]);
-              c3[4 * q4 + 3] = fmaf(d, v3.w, c3[4 * q4 + 3]);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) corr_s[(16 + j) * CC + c] = c3[j];
-        }
-        named_sync_dec();  // sub-block 2 decided; corrections of 3 out
       }
-      if (lane == 0) stamp(a, t, 20 + warp);
+      tc::fence_before_sync();
       named_sync_128();
-      if (threadIdx.x == 0) {
-        stamp(a, t, 4);
-        mbar_arrive(sh.a_full);
-        mbar_arrive(&sh.jbb_free[t & 1]);
-        mbar_arrive(&sh.lf_free[t & 1]);
+      if (threadIdx.x == 0) stamp_cta(a, 3);
+      if (q == 0 && valid && !*sh.abort) {
+        a.s.energies[chain] = (float)e0_s[c];
+        for (int w = 0; w < words; ++w)
+          a.s.spins[chain * a.p.words + w] = spins_s[w * CC + c];
       }
-    }
-    // ----------------------------------------------------------- epilogue
-    if (!*sh.abort && NB > 0)
-      tc_wait(sh.mma_done, (NB - 1) & 1, sh, status);
-    tc::fence_after_sync();
-    if (threadIdx.x == 0) stamp_cta(a, NB, 2);
-    if (__all_sync(0xffffffffu, !*sh.abort)) {
-      for (int j0 = 0; j0 < S; j0 += 32) {
-        float v[32];
-        tc::tmem_ld32(taddr + lane_base + j0, v);
+    } else if (warp == 4) {
+      // ============================================================== MMA
+      if (lane == 0) {
+        // rows [r_lo, r_hi) of the 256-row B tile in `slot` against A slice
+        // qq, into the field columns 256 j + r_lo ...
+        auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi,
+                            uint32_t acc) {
+          if (r_hi <= r_lo) return;
+          const uint32_t idesc = r_hi - r_lo == 256
+                                     ? idesc_full
+                                     : tc::idesc_bf16(128, r_hi - r_lo);
+          const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
+          const uint32_t b0 = smem_base +
+                              (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
+                              (uint32_t)(r_lo / 8) * 1024u;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) stg[lane * 33 + i] = v[i];
-        __syncwarp();
-        const int col = w_q * S + j0 + 4 * (lane & 7);
-#pragma unroll
-        for (int it = 0; it < 8; ++it) {
-          const int rr = 4 * it + (lane >> 3);
-          const int cr = w_c0 + rr;
-          if (cr < item.nchains && col < n) {
-            const float* sv = stg + rr * 33 + 4 * (lane & 7);
-            float* f = a.fields + (item.chain0 + cr) * (int64_t)a.field_ld + col;
-            if (col + 4 <= n) {
-              *reinterpret_cast<float4*>(f) =
-                  make_float4(sv[0], sv[1], sv[2], sv[3]);
-            } else {
-              f[0] = sv[0];
-              if (col + 1 < n) f[1] = sv[1];
-              if (col + 2 < n) f[2] = sv[2];
-            }
-          }
-        }
-        __syncwarp();
-      }
-    }
-    tc::fence_before_sync();
-    named_sync_128();
-    if (threadIdx.x == 0) stamp_cta(a, NB, 3);
-    if (q == 0 && valid && !*sh.abort) {
-      const float e_new = (float)(e0_s[c] + dE_s[c]);
-      a.s.energies[chain] = e_new;
-      const bool improved = e_new < a.s.best_energy[chain];
-      if (improved) {
-        a.s.best_energy[chain] = e_new;
-        a.s.best_sweep[chain] = (int32_t)sweep;
-      }
-      for (int w = 0; w < words; ++w) {
-        const uint32_t v = spins_s[w * CC + c];
-        a.s.spins[chain * a.p.words + w] = v;
-        if (improved) a.s.best_spins[chain * a.p.words + w] = v;
-      }
-    }
-  } else if (warp == 4) {
-    // ============================================================== MMA
-    if (lane == 0) {
-      uint32_t u = 0;
-      for (int t = 0; rc && t < NB; ++t) {
-        if (!tc_wait(sh.rc_full, t & 1, sh, status)) break;
-        tc::fence_after_sync();
+          for (int ks = 0; ks < 4; ++ks)
+            tc::mma_bf16(taddr + 256 * j + r_lo,
+                         tc::smem_desc(a0 + 256 * ks, 128, 1024),
+                         tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc,
+                         (acc | (uint32_t)ks) ? 1u : 0u);
+        };
         bool ok = true;
-        for (int j = 0; j < NT && ok; ++j) {
-          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-          const uint32_t idesc =
-              width == 256 ? idesc_full : tc::idesc_bf16(128, width);
-          for (int term = 0; term < T && ok; ++term) {
-            for (int qq = 0; qq < F; ++qq) {
-              const uint32_t slot = u % C::NS;
-              if (!tc_wait(&sh.full[slot], (u / C::NS) & 1, sh, status)) {
+        for (int s = 0; s < KU && ok; ++s) {
+          if (rc_at(s)) {
+            for (int t = 0; t < NB && ok; ++t) {
+              if (!tc_wait(sh.rc_full, RG & 1, sh, status)) {
                 ok = false;
                 break;
               }
               tc::fence_after_sync();
-              const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
-              const uint32_t b0 =
-                  smem_base + (uint32_t)(C::B_OFF + slot * C::B_STAGE);
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks)
-                tc::mma_bf16(taddr + 256 * j,
-                             tc::smem_desc(a0 + 256 * ks, 128, 1024),
-                             tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc,
-                             (t | term | qq | ks) ? 1u : 0u);
-              tc::commit(&sh.free_[slot]);
-              ++u;
+              for (int j = 0; j < NT && ok; ++j) {
+                const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+                for (int term = 0; term < T && ok; ++term) {
+                  for (int qq = 0; qq < F; ++qq) {
+                    const uint32_t slot = u % C::NS;
+                    if (!tc_wait(&sh.full[slot], (u / C::NS) & 1, sh, status)) {
+                      ok = false;
+                      break;
+                    }
+                    tc::fence_after_sync();
+                    mma_rows(slot, qq, j, 0, width,
+                             (t | term | qq) ? 1u : 0u);
+                    tc::commit(&sh.free_[slot]);
+                    ++u;
+                  }
+                }
+              }
+              if (!ok) break;
+              tc::commit(sh.rc_done);
+              ++RG;
             }
           }
-        }
-        if (!ok) break;
-        tc::commit(sh.rc_done);
-      }
-      // rows [r_lo, r_hi) of the 256-row B tile in `slot` against A slice
-      // qq, into the field columns 256 j + r_lo ...
-      auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi) {
-        if (r_hi <= r_lo) return;
-        const uint32_t idesc =
-            r_hi - r_lo == 256 ? idesc_full : tc::idesc_bf16(128, r_hi - r_lo);
-        const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
-        const uint32_t b0 = smem_base +
-                            (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
-                            (uint32_t)(r_lo / 8) * 1024u;
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks)
-          tc::mma_bf16(taddr + 256 * j + r_lo,
-                       tc::smem_desc(a0 + 256 * ks, 128, 1024),
-                       tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc, 1u);
-      };
-      for (int t = 0; t < NB; ++t) {
-        if (!tc_wait(sh.a_full, t & 1, sh, status)) break;
-        stamp(a, t, 5);
-        tc::fence_after_sync();
-        // the next block's 64 columns: slice qn, tile jf, rows r0 .. r0+63
-        const bool has_next = t + 1 < NB;
-        const int cn = has_next ? (64 * (t + 1)) % S : 0;
-        const int qn = has_next ? (64 * (t + 1)) / S : 0;
-        const int jf = cn / 256, r0 = cn % 256;
-        bool ok = true;
-        for (int jj = 0; jj < NT && ok; ++jj) {
-          const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
-          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-          // stage order: slices from qn on, terms inside (the producer
-          // issues the same order)
-          for (int k = 0; k < F && ok; ++k) {
-            const int qq = (qn + k) % F;
-            const bool crit = jj == 0 && k == 0 && has_next;
-            for (int term = 0; term < T; ++term) {
-              const uint32_t slot = (u + term) % C::NS;
-              if (!tc_wait(&sh.full[slot], ((u + term) / C::NS) & 1, sh,
-                           status)) {
-                ok = false;
-                break;
+          for (int t = 0; t < NB && ok; ++t) {
+            const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
+            if (!tc_wait(sh.a_full, Gb & 1, sh, status)) {
+              ok = false;
+              break;
+            }
+            stamp(a, Gb, 5);
+            tc::fence_after_sync();
+            // the next block's 64 columns (next sweep's first block after the
+            // last): slice qn, tile jf, rows r0 .. r0+63
+            const bool has_next = Gb + 1 < Gend;
+            const int tn = (t + 1) % NB;
+            const int cn = (64 * tn) % S, qn = (64 * tn) / S;
+            const int jf = has_next ? cn / 256 : 0, r0 = cn % 256;
+            for (int jj = 0; jj < NT && ok; ++jj) {
+              const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
+              const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+              // stage order: slices from qn on, terms inside (the producer
+              // issues the same order)
+              for (int k = 0; k < F && ok; ++k) {
+                const int qq = (qn + k) % F;
+                const bool crit = jj == 0 && k == 0 && has_next;
+                for (int term = 0; term < T; ++term) {
+                  const uint32_t slot = (u + term) % C::NS;
+                  if (!tc_wait(&sh.full[slot], ((u + term) / C::NS) & 1, sh,
+                               status)) {
+                    ok = false;
+                    break;
+                  }
+                  tc::fence_after_sync();
+                  if (crit)
+                    mma_rows(slot, qq, j, r0, r0 + 64, 1u);
+                  else
+                    mma_rows(slot, qq, j, 0, width, 1u);
+                }
+                if (!ok) break;
+                if (crit) {
+                  // the next block's decisions may start once these land
+                  tc::commit(sh.h_ready);
+                  stamp(a, Gb, 6);
+                  for (int term = 0; term < T; ++term) {
+                    const uint32_t slot = (u + term) % C::NS;
+                    mma_rows(slot, qq, j, 0, r0, 1u);
+                    mma_rows(slot, qq, j, r0 + 64, width, 1u);
+                  }
+                }
+                for (int term = 0; term < T; ++term)
+                  tc::commit(&sh.free_[(u + term) % C::NS]);
+                u += T;
               }
-              tc::fence_after_sync();
-              if (crit)
-                mma_rows(slot, qq, j, r0, r0 + 64);
-              else
-                mma_rows(slot, qq, j, 0, width);
             }
             if (!ok) break;
-            if (crit) {
-              // the next block's decisions may start once these land
-              tc::commit(sh.h_ready);
-              stamp(a, t, 6);
-              for (int term = 0; term < T; ++term) {
-                const uint32_t slot = (u + term) % C::NS;
-                mma_rows(slot, qq, j, 0, r0);
-                mma_rows(slot, qq, j, r0 + 64, width);
-              }
-            }
-            for (int term = 0; term < T; ++term)
-              tc::commit(&sh.free_[(u + term) % C::NS]);
-            u += T;
+            if (!has_next) tc::commit(sh.h_ready);  // one phase per block
+            tc::commit(sh.mma_done);
           }
         }
-        if (!ok) break;
-        tc::commit(sh.mma_done);
+        if (!ok) *sh.abort = 1;
       }
-    }
-  } else if (warp == 5) {
-    // ========================================================= producer
-    if (lane == 0) {
-      const uint16_t* B = a.tc_b + item.b_off;
-      const float* D = a.tc_diag + item.diag_off;
-      const size_t tile_elems = 256 * 64;
-      auto issue_jbb = [&](int t) {
-        uint64_t* bar = &sh.jbb_full[t & 1];
-        mbar_expect_tx_arrive(bar, 16384);
-        bulk_g2s(smem + C::JBB_OFF + (t & 1) * 16384, D + (size_t)t * 4096,
-                 16384, bar);
-      };
-      if (NB > 0) issue_jbb(0);
-      if (NB > 1) issue_jbb(1);
-      uint32_t u = 0;
-      for (int t = 0; rc && t < NB && !*sh.abort; ++t) {
-        bool ok = true;
-        for (int j = 0; j < NT && ok; ++j) {
+    } else if (warp == 5) {
+      // ========================================================= producer
+      if (lane == 0) {
+        const uint16_t* Bp = a.tc_b + item.b_off;
+        const float* D = a.tc_diag + item.diag_off;
+        const size_t tile_elems = 256 * 64;
+        // diagonal block of global block Gx (block (Gx - G0) % NB of the
+        // unit) into buffer Gx & 1, once block Gx - 2 has released it
+        auto issue_jbb = [&](uint32_t Gx) {
+          if (Gx >= 2 &&
+              !tc_wait(&sh.jbb_free[Gx & 1], ((Gx >> 1) - 1) & 1, sh, status))
+            return false;
+          const int tx = (int)((Gx - G0) % (uint32_t)NB);
+          uint64_t* bar = &sh.jbb_full[Gx & 1];
+          mbar_expect_tx_arrive(bar, 16384);
+          bulk_g2s(smem + C::JBB_OFF + (Gx & 1) * 16384, D + (size_t)tx * 4096,
+                   16384, bar);
+          return true;
+        };
+        auto issue_stage = [&](int t, int term, int qq, int j) {
+          const uint32_t slot = u % C::NS;
+          if (u >= (uint32_t)C::NS &&
+              !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh, status))
+            return false;
           const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-          for (int term = 0; term < T && ok; ++term) {
-            for (int qq = 0; qq < F; ++qq) {
-              const uint32_t slot = u % C::NS;
-              if (u >= (uint32_t)C::NS &&
-                  !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh,
-                           status)) {
-                ok = false;
-                break;
-              }
-              const size_t src =
-                  ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
-              const uint32_t bytes = (uint32_t)width * 128;
-              mbar_expect_tx_arrive(&sh.full[slot], bytes);
-              bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, B + src, bytes,
-                       &sh.full[slot]);
-              ++u;
+          const size_t src =
+              ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
+          const uint32_t bytes = (uint32_t)width * 128;
+          mbar_expect_tx_arrive(&sh.full[slot], bytes);
+          bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, Bp + src, bytes,
+                   &sh.full[slot]);
+          ++u;
+          return true;
+        };
+        bool ok = issue_jbb(G0);
+        for (int s = 0; s < KU && ok; ++s) {
+          if (rc_at(s)) {
+            for (int t = 0; t < NB && ok; ++t)
+              for (int j = 0; j < NT && ok; ++j)
+                for (int term = 0; term < T && ok; ++term)
+                  for (int qq = 0; qq < F && ok; ++qq)
+                    ok = issue_stage(t, term, qq, j);
+          }
+          for (int t = 0; t < NB && ok; ++t) {
+            const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
+            // the next block's diagonal block lands while this one is decided
+            if (Gb + 1 < Gend) ok = issue_jbb(Gb + 1);
+            const bool has_next = Gb + 1 < Gend;
+            const int tn = (t + 1) % NB;
+            const int jf = has_next ? ((64 * tn) % S) / 256 : 0;
+            const int qn = (64 * tn) / S;
+            for (int jj = 0; jj < NT && ok; ++jj) {
+              const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
+              for (int k = 0; k < F && ok; ++k)
+                for (int term = 0; term < T && ok; ++term)
+                  ok = issue_stage(t, term, (qn + k) % F, j);
             }
+            stamp(a, Gb, 7);
           }
         }
-        if (!ok) break;
+        if (!ok) *sh.abort = 1;
       }
-      for (int t = 0; t < NB && !*sh.abort; ++t) {
-        // the next block's diagonal block, into the buffer block t-1 used:
-        // it lands while block t is being decided
-        if (t >= 1 && t + 1 < NB) {
-          if (!tc_wait(&sh.jbb_free[(t + 1) & 1], (((t + 1) >> 1) - 1) & 1,
-                       sh, status))
-            break;
-          issue_jbb(t + 1);
-        }
-        const bool has_next = t + 1 < NB;
-        const int jf = has_next ? ((64 * (t + 1)) % S) / 256 : 0;
-        const int qn = has_next ? (64 * (t + 1)) / S : 0;
-        bool ok = true;
-        for (int jj = 0; jj < NT && ok; ++jj) {
-          const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
-          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-          for (int k = 0; k < F && ok; ++k) {
-            const int qq = (qn + k) % F;
-            for (int term = 0; term < T; ++term) {
-              const uint32_t slot = u % C::NS;
-              if (u >= (uint32_t)C::NS &&
-                  !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh,
-                           status)) {
-                ok = false;
-                break;
-              }
-              const size_t src =
-                  ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
-              const uint32_t bytes = (uint32_t)width * 128;
-              mbar_expect_tx_arrive(&sh.full[slot], bytes);
-              bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, B + src, bytes,
-                       &sh.full[slot]);
-              ++u;
-            }
-          }
-        }
-        if (!ok) break;
-        stamp(a, t, 7);
-      }
-    }
-  }
-
-  if (warp >= 6) {
-    // ======================================== log-uniforms of the next block
-    const int hid = threadIdx.x - 192;
-    for (int t = 0; t < NB; ++t) {
-      bool go = !*sh.abort;
-      if (go && t >= 2)
-        go = tc_wait(&sh.lf_free[t & 1], ((t >> 1) - 1) & 1, sh, status);
-      if (go) {
-        float* out = lf_s + (t & 1) * 64 * CC;
-        for (int it = hid; it < CC * 16; it += 64) {
-          const int c2 = it % CC, quad = it / CC;
-          const uint32_t cl =
-              (uint32_t)(item.chain0 + c2 - chain_base);
-          uint32_t x[4];
-          draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, cl,
-                (uint32_t)(16 * t + quad), x);
+    } else {
+      // ================================= log-uniforms of the next blocks
+      const int hid = threadIdx.x - 192;
+      for (int s = 0; s < KU; ++s) {
+        const uint32_t sweep = sweep_first + (uint32_t)s;
+        for (int t = 0; t < NB; ++t) {
+          const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
+          bool go = !*sh.abort;
+          if (go && Gb >= 2)
+            go = tc_wait(&sh.lf_free[Gb & 1], ((Gb >> 1) - 1) & 1, sh, status);
+          if (go) {
+            float* out = lf_s + (Gb & 1) * 64 * CC;
+            for (int it = hid; it < CC * 16; it += 64) {
+              const int c2 = it % CC, quad = it / CC;
+              const uint32_t cl = (uint32_t)(item.chain0 + c2 - chain_base);
+              uint32_t x[4];
+              draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, cl,
+                    (uint32_t)(16 * t + quad), x);
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
-            out[(4 * quad + e) * CC + c2] = log_uniform_f32(x[e]);
+              for (int e = 0; e < 4; ++e)
+                out[(4 * quad + e) * CC + c2] = log_uniform_f32(x[e]);
+            }
+          }
+          named_sync_helpers();
+          if (hid == 0) mbar_arrive(&sh.lf_full[Gb & 1]);
         }
       }
-      named_sync_helpers();
-      if (hid == 0) mbar_arrive(&sh.lf_full[t & 1]);
+    }
+
+    // ------------------------------------------------------- unit end
+    __threadfence();  // this unit's global stores before its done flag
+    G = Gend;
+    RG = RG0 + (uint32_t)(n_rc * NB);
+    __syncwarp();  // single-lane roles (MMA, producer) rejoin their warps
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (threadIdx.x == 0) {
+      stamp_cta(a, 4);
+      __threadfence();  // this unit's stores before its done flag
+      atomicExch(reinterpret_cast<int*>(a.sched + 2 + un % a.num_items),
+                 chunk + 1);
     }
   }
 
-  __syncwarp();  // single-lane roles (MMA, producer) rejoin their warps
+  // ------------------------------------------------------------ teardown
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const uint32_t fin = atomicAdd(reinterpret_cast<unsigned*>(a.sched + 1), 1u);
+    if (fin == gridDim.x - 1 && a.advance_counter)
+      *a.s.sweep_counter += (int64_t)a.unit_sweeps * a.units_per_item;
+  }
+  __syncwarp();
   tc::fence_before_sync();
   __syncthreads();
-  if (threadIdx.x == 0) stamp_cta(a, NB, 4);
   if (warp == 0) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(taddr, ncols);
+    tc::tmem_dealloc(taddr, kCols);
   }
 }
 
@@ -951,8 +1094,10 @@ static cudaError_t launch_tc_t(const TcArgs& a, int count, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc(const TcArgs& a, int F, int count, cudaStream_t st) {
-  if (count <= 0) return cudaSuccess;
+cudaError_t launch_tc(const TcArgs& a, int F, int max_ctas, cudaStream_t st) {
+  const int64_t units = (int64_t)a.num_items * a.units_per_item;
+  if (units <= 0) return cudaSuccess;
+  const int count = (int)(units < max_ctas ? units : max_ctas);
   switch (F) {
     case 1: return launch_tc_t<1>(a, count, st);
     case 2: return launch_tc_t<2>(a, count, st);

@@ -25,8 +25,16 @@ struct TcArgs {
   const TcItem* items;
   uint64_t seed;
   int32_t recompute_every;  // >0: H and E rebuilt when sweep % this == 0
+  int32_t num_items;        // items of this fold
+  int32_t unit_sweeps;      // sweeps per work unit
+  int32_t units_per_item;   // work units per item in this launch
+  int32_t fuse_exchange;    // 1: exchange inside the kernel (R | chains/CTA)
+  int32_t use_pt;
+  int32_t advance_counter;  // 1: the last CTA advances the sweep counter
   int32_t pad_;
-  // optional timeline of CTA 0 (globaltimer ns): [block][8] stamps
+  int32_t* sched;  // zeroed per launch: [0] unit queue, [1] finished CTAs,
+                   // [2 + item] units of the item done
+  // optional timeline of CTA 0 (globaltimer ns): [49][24] stamps
   unsigned long long* trace;
 };
 
@@ -36,6 +44,8 @@ int64_t tc_b_elems(int n, int terms);
 int64_t tc_diag_elems(int n);
 cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
                            uint16_t* b_out, float* diag_out, cudaStream_t st);
-cudaError_t launch_tc(const TcArgs& a, int F, int count, cudaStream_t st);
+// Persistent launch over a.num_items * a.units_per_item work units with at
+// most `max_ctas` CTAs; a.sched must hold 2 + num_items zeroed words.
+cudaError_t launch_tc(const TcArgs& a, int F, int max_ctas, cudaStream_t st);
 
 }  // namespace pysa_gb

@@ -210,6 +210,7 @@ class PTBatch:
             self.tc_diag = z(max(int(tneed[1]), 1), torch.float32)
             self.tc_items = z(max(int(tneed[2]), 8), torch.int32)
             self.tc_inst = z(max(I, 1), torch.int32)
+            self.tc_sched = z(2 + max(titems, 1), torch.int32)
             self.ws.tc_b = _ptr(self.tc_b)
             self.ws.tc_b_elems = int(tneed[0])
             self.ws.tc_diag = _ptr(self.tc_diag)
@@ -217,6 +218,7 @@ class PTBatch:
             self.ws.tc_items = _ptr(self.tc_items)
             self.ws.tc_num_items = max(titems, 1)
             self.ws.tc_inst = _ptr(self.tc_inst)
+            self.ws.tc_sched = _ptr(self.tc_sched)
             self.ws.tc_terms = terms
             self.tc_terms = terms
         self.ws.tc_min_n = int(min_n)
