@@ -791,7 +791,9 @@ def main():
         tp = os.path.join(ROOT, "profiles", "sweep_plain_qubo1024_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            roof["traffic"] = json.load(f).get("bytes_per_launch")
+            tj = json.load(f)
+            # per sweep, like `achieved` (one ncu capture of a 32-sweep launch)
+            roof["traffic"] = tj.get("bytes_per_sweep", tj.get("bytes_per_launch"))
 
     # end to end through the public API (host buffers in and out)
     e2e = None
