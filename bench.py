@@ -777,7 +777,8 @@ def main():
                 "kernel": f"k_sweep_tc<{fold}>", "bf16_terms": terms,
                 "issued_flop_per_launch": alg * fold,
                 "alg_flop_per_launch": alg, "sweep_ms": sweep_s * 1e3}
-        tp = os.path.join(ROOT, "profiles", "sweep_tc_qubo1024_traffic.json")
+        tp = os.path.join(ROOT, "profiles",
+                          f"sweep_tc_{args.workload}_traffic.json")
     else:
         # algorithmic bytes of one launch: fields read+write, spins
         # read+write, J once
@@ -788,7 +789,8 @@ def main():
                 "peak_source": peak_kind, "kernel": "k_sweep_plain<32,4,8,8>",
                 "alg_bytes_per_launch": int(alg_bytes),
                 "sweep_ms": sweep_s * 1e3}
-        tp = os.path.join(ROOT, "profiles", "sweep_plain_qubo1024_traffic.json")
+        tp = os.path.join(ROOT, "profiles",
+                          f"sweep_plain_{args.workload}_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
