@@ -606,6 +606,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="qubo1024", choices=list(WORKLOADS))
+    ap.add_argument("--kernel", default="auto",
+                    choices=["auto", "tc", "plain", "autotune"],
+                    help="sweep kernel of the single-instance workloads")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-sweeps", type=int, default=None)
@@ -645,7 +648,11 @@ def main():
     J = P.copy()
     np.fill_diagonal(J, 0)
     R, Rd, n = w["replicas"], w["reads"], w["n"]
-    batch = PTBatch(ptype, [Instance(J, h, ladder(w), Rd)], kernel="auto")
+    batch = PTBatch(ptype, [Instance(J, h, ladder(w), Rd)], kernel=args.kernel)
+    if args.kernel == "autotune":
+        batch.set_states(pack_spins(
+            np.zeros((Rd, R, n), np.float32), ptype, batch.words), None)
+        batch.autotune()
     use_tc = batch.tc and w["update"] == "sequential"
     rng = np.random.default_rng(100 + rank)
     if ptype == "qubo":
@@ -848,6 +855,8 @@ def main():
                               "memory within a launch" % chunk) if fused else
                              "flushed (256 MB write) before every step",
                        "sweeps_per_launch": chunk,
+                       "kernel_choice": args.kernel,
+                       "tc_min_n": batch.tc_min_n,
                        "kernel": ("persistent tensor-core blocked sweep "
                                   "(tcgen05, split-BF16%s)" %
                                   (", exchange fused" if fused else ""))

@@ -239,6 +239,40 @@ static inline bool tc_selected(int n, int min_n) {
   return n >= (min_n < 64 ? 64 : min_n) && n <= 2048;
 }
 
+// Chains per tensor-core work item of every selected instance: a CTA's full
+// tensor memory (128/F chains), halved while the batch would fill fewer
+// CTAs than the GPU has SMs and the halves still hold whole reads (or whole
+// warps when R does not divide 128/F).  0 for instances left to the plain
+// kernel.
+static std::vector<int> tc_item_sizes(int num_instances,
+                                      const pysa_gb_host_tables* host,
+                                      int min_n) {
+  std::vector<int> size(num_instances, 0), gran(num_instances, 32);
+  for (int i = 0; i < num_instances; ++i) {
+    if (!tc_selected(host->n[i], min_n)) continue;
+    size[i] = tc_chains_per_cta(host->n[i]);
+    if (size[i] % host->replicas[i] == 0) gran[i] = host->replicas[i];
+  }
+  const int sms = sm_count();
+  for (;;) {
+    int64_t items = 0;
+    bool can = false;
+    for (int i = 0; i < num_instances; ++i) {
+      if (!size[i]) continue;
+      const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
+      items += (chains + size[i] - 1) / size[i];
+      const int h = size[i] / 2;
+      can |= h >= gran[i] && h % gran[i] == 0;
+    }
+    if (items >= sms || !can) break;
+    for (int i = 0; i < num_instances; ++i) {
+      const int h = size[i] / 2;
+      if (size[i] && h >= gran[i] && h % gran[i] == 0) size[i] = h;
+    }
+  }
+  return size;
+}
+
 int pysa_gb_tc_workspace(int32_t num_instances,
                          const pysa_gb_host_tables* host, int32_t terms,
                          int32_t min_n, int64_t out[3]) {
@@ -246,6 +280,10 @@ int pysa_gb_tc_workspace(int32_t num_instances,
       (num_instances > 0 && (!host || !host->n || !host->replicas ||
                              !host->reads)))
     return fail(PYSA_GB_ERR_ARG, "tc_workspace: bad argument");
+  for (int i = 0; i < num_instances; ++i)
+    if (host->replicas[i] < 1 || host->reads[i] < 0)
+      return fail(PYSA_GB_ERR_ARG, "tc_workspace: bad replicas or reads");
+  const std::vector<int> isz = tc_item_sizes(num_instances, host, min_n);
   int64_t b = 0, d = 0, items = 0;
   for (int i = 0; i < num_instances; ++i) {
     const int n = host->n[i];
@@ -253,8 +291,7 @@ int pysa_gb_tc_workspace(int32_t num_instances,
     b += tc_b_elems(n, terms);
     d += tc_diag_elems(n);
     const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
-    const int cc = tc_chains_per_cta(n);
-    items += (chains + cc - 1) / cc;
+    items += (chains + isz[i] - 1) / isz[i];
   }
   out[0] = b;
   out[1] = d;
@@ -294,13 +331,14 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     dd += tc_diag_elems(host->n[i]);
   }
   std::vector<TcItem> items;
+  const std::vector<int> isz = tc_item_sizes(p->num_instances, host, min_n);
   const int folds[3] = {1, 2, 4};
   for (int v = 0; v < 3; ++v) {
     ws->tc_variant_start[v] = (int32_t)items.size();
     for (int i = 0; i < p->num_instances; ++i) {
       if (!flags[i] || tc_fold_for(host->n[i]) != folds[v]) continue;
       const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
-      const int cc = tc_chains_per_cta(host->n[i]);
+      const int cc = isz[i];
       for (int64_t c = 0; c < chains; c += cc) {
         TcItem it;
         it.inst = i;

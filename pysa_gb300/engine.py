@@ -67,7 +67,7 @@ class PTBatch:
         """kernel: 'plain' (CUDA-core sweep for every instance), 'tc'
         (tensor-core blocked sweep for every instance, sequential order,
         64 <= n <= 2048), 'auto' (tensor cores for the instances with
-        256 <= n <= 2048, the plain kernel for the rest, in the same sweep)
+        64 <= n <= 2048, the plain kernel for the rest, in the same sweep)
         or 'autotune' ('auto' until autotune() picks the threshold by
         timing; run() calls it on first use)."""
         if not torch.cuda.is_available():
@@ -183,8 +183,8 @@ class PTBatch:
                                  "every instance")
             self._setup_tc(64)
         elif kernel in ("auto", "autotune"):
-            if I and ((n >= 256) & (n <= 2048)).any():
-                self._setup_tc(256)
+            if I and ((n >= 64) & (n <= 2048)).any():
+                self._setup_tc(64)
         elif kernel != "plain":
             raise ValueError(f"unknown kernel {kernel!r}")
         self.autotune_pending = kernel == "autotune"

@@ -129,7 +129,7 @@ def test_tc_recompute_keeps_integer_trajectory(oracle, every):
 
 @pytest.mark.parametrize("kernel", ["auto", "autotune"])
 def test_mixed_tc_and_plain_batch_bit_exact(oracle, kernel):
-    """One batch where instances with n >= 256 take the tensor-core sweep
+    """One batch where instances with n >= 64 take the tensor-core sweep
     and the others the plain kernel in the same sweep (kernel='auto'), or
     whatever split the autotuner picks: every instance must still follow
     the oracle bit for bit, and tuning must not change the chains."""
@@ -143,7 +143,7 @@ def test_mixed_tc_and_plain_batch_bit_exact(oracle, kernel):
         insts.append(Instance(J, h, betas, Rd))
         x0s.append(rng.integers(0, 2, (Rd, R, n)).astype(np.float32))
     b = PTBatch("qubo", insts, kernel=kernel)
-    assert b.tc and b.tc_min_n == 256
+    assert b.tc and b.tc_min_n == 64
     words = b.words
     b.set_states(np.concatenate([pack_spins(x, "qubo", words).reshape(-1, words)
                                  for x in x0s]), None)
