@@ -681,10 +681,11 @@ def main():
                         device="cuda")
     # With every instance on the tensor cores and R dividing the chains per
     # CTA, a launch runs several sweeps with the exchange fused in and the
-    # fields resident in tensor memory: time launches of 32 sweeps (L2
-    # flushed before each).  Otherwise time each sweep and its exchange.
+    # fields resident in tensor memory: time launches of 64 sweeps (the
+    # library's launch size; L2 flushed before each).  Otherwise time each
+    # sweep and its exchange.
     fused = bool(use_tc and batch.ws.plain_live == 0 and batch.ws.tc_fusable)
-    chunk = 32 if fused else 1
+    chunk = 64 if fused else 1
     iters = []
     done = 0
     while done < args.steps:

@@ -142,8 +142,8 @@ typedef struct {
                                per CTA (exchange can run inside the kernel) */
   int32_t *tc_sched;        /* [2 + tc_num_items] device scratch of the
                                persistent tensor-core kernel */
-  int32_t tc_unit_sweeps;   /* sweeps per work unit of that kernel (0: 4) */
-  int32_t pad_;
+  int32_t tc_unit_sweeps;   /* sweeps per work unit of that kernel (0: 8) */
+  int32_t tc_launch_sweeps; /* most sweeps one launch of it covers (0: 64) */
 } pysa_gb_workspace;
 
 /* Host copies of the per-instance tables, used to plan the work list. */

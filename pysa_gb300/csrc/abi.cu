@@ -64,8 +64,8 @@ static int cuda_fail(cudaError_t e, const char* where) {
               std::string(where) + ": " + cudaGetErrorString(e));
 }
 
-// Most sweeps one fused tensor-core launch covers.
-constexpr int kMaxFusedSweeps = 32;
+// Default for the most sweeps one fused tensor-core launch covers.
+constexpr int kMaxFusedSweeps = 64;
 
 // Streaming multiprocessors of the current device (cached per device).
 static int sm_count() {
@@ -497,10 +497,12 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
                      o->log_omega_stride == 0 &&
                      (!o->use_pt || ws->tc_fusable) && ws->tc_sched;
   if (fused) {
-    const int ku_pref = ws->tc_unit_sweeps > 0 ? ws->tc_unit_sweeps : 4;
+    const int ku_pref = ws->tc_unit_sweeps > 0 ? ws->tc_unit_sweeps : 8;
+    const int per_launch =
+        ws->tc_launch_sweeps > 0 ? ws->tc_launch_sweeps : kMaxFusedSweeps;
     int remaining = num_sweeps;
     while (remaining > 0) {
-      int chunk = remaining < kMaxFusedSweeps ? remaining : kMaxFusedSweeps;
+      int chunk = remaining < per_launch ? remaining : per_launch;
       const int ku = chunk < ku_pref ? chunk : ku_pref;
       chunk = chunk / ku * ku;
       const int rc = tc_launches(ku, chunk / ku, 1);
