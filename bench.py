@@ -485,9 +485,36 @@ def run_ais_workload(args, w, rank, world):
                       "max_abs_err": float(np.abs(err).max()),
                       "attempts_per_s":
                           I * w["samples"] * w["temps"] * n / dt}
+    # all instances in one launch (engine.run_ais_batch), same estimator:
+    # log Z = omegas_to_partition(log w, n log 2)
+    from pysa_gb300.engine import run_ais_batch
+    from pysa_gb300.ais import omegas_to_partition
+    temps = np.array([(i + 1) / w["temps"] for i in range(w["temps"])],
+                     np.float32)
+    srng = np.random.default_rng(77)
+    batch_in = [((w["beta"] * P).astype(np.float32), np.zeros(n, np.float32),
+                 (2 * srng.integers(0, 2, (w["samples"], n)) - 1
+                  ).astype(np.float32)) for P in probs]
+    run_ais_batch("ising", batch_in[:2], temps[:4], seed=0)  # warm-up
+    torch.cuda.synchronize()
+    bt = []
+    for rep in range(3):
+        t0 = time.perf_counter()
+        res = run_ais_batch("ising", batch_in, temps, seed=500 + rep,
+                            update="sequential")
+        bt.append(time.perf_counter() - t0)
+    est = [omegas_to_partition(lw, n * np.log(2.0)) for _, lw in res]
+    err = np.asarray(est) - exact
+    attempts = I * w["samples"] * w["temps"] * n
+    out["batched_reference_order"] = {
+        "seconds": min(bt), "attempts_per_s": attempts / min(bt),
+        "mean_err": float(err.mean()), "max_abs_err": float(np.abs(err).max()),
+        "includes": "state upload, field set-up, the AIS launch, samples and "
+                    "weights download (host buffers in and out)"}
     print(json.dumps({
         "metric": "ais_attempts_per_s",
-        "value": out["reference"]["attempts_per_s"], "unit": "attempts/s",
+        "value": out["batched_reference_order"]["attempts_per_s"],
+        "unit": "attempts/s",
         "n_gpus": 1, "steps": I, "warmup": 1, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 weights)",
         "data": "synthetic (seeded)",
@@ -498,9 +525,12 @@ def run_ais_workload(args, w, rank, world):
         "exact": {"seconds": t_exact,
                   "states_per_s": I * 2.0**n / t_exact,
                   "logz_mean": float(np.mean(exact))},
-        "e2e": {"value": out["reference"]["attempts_per_s"],
-                "unit": "attempts/s", "h2d_bytes_per_step": n * n * 8,
-                "d2h_bytes_per_step": w["samples"] * (n + 8) * 4}}),
+        "e2e": {"value": out["batched_reference_order"]["attempts_per_s"],
+                "unit": "attempts/s", "h2d_bytes_per_step": I * (
+                    n * n * 4 + w["samples"] * 4 * ((n + 31) // 32)),
+                "d2h_bytes_per_step": I * w["samples"] * (
+                    4 * ((n + 31) // 32) + 8),
+                "per_instance_solver": out["reference"]["attempts_per_s"]}}),
         flush=True)
     return 0
 

@@ -260,10 +260,14 @@ int pysa_gb_unpack(int32_t problem_type, int32_t n, const uint32_t *spins,
 
 /* Annealed importance sampling (Solver.annealed_importance, pysa/sa.py:432-553;
  * ais_sample, pysa/simulation.py:293-317; update_spin_ref,
- * pysa/ising.py:66-92).  One instance; state.spins holds the initial samples
- * [samples, words], state.energies their energies and ws.fields their local
- * fields (from pysa_gb_prepare, with the couplings already scaled by the
- * target beta).  Writes final samples, energies and the f64 log weights. */
+ * pysa/ising.py:66-92).  Every instance of the batch (one replica each; its
+ * reads are its samples) anneals in one launch on the same temperature
+ * schedule; state.spins holds the initial samples [chains, words],
+ * state.energies their energies and ws.fields their local fields (from
+ * pysa_gb_prepare, with the couplings already scaled by the target beta).
+ * Writes final samples, energies and the f64 log weights [chains].  Random
+ * order needs ws.perm_slots >= num_temps.  An instance with more than one
+ * replica sets PYSA_GB_ERR_ARG in the status word. */
 typedef struct {
   uint64_t seed;
   int32_t update;     /* PYSA_GB_SEQUENTIAL or PYSA_GB_RANDOM */
@@ -273,6 +277,8 @@ typedef struct {
                          1: weight before each sweep (standard AIS) */
   int32_t num_temps;
   double p;           /* bernoulli: probability of bit 0 / spin -1 */
+  int32_t max_samples;/* largest reads of an instance (0: num_chains) */
+  int32_t pad_;
 } pysa_gb_ais_options;
 
 int pysa_gb_ais(const pysa_gb_problems *p, pysa_gb_state *s,

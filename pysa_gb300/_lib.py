@@ -77,7 +77,8 @@ class ProposalScratch(ctypes.Structure):
 
 class AisOptions(ctypes.Structure):
     _fields_ = [("seed", U64), ("update", I32), ("reference", I32),
-                ("order", I32), ("num_temps", I32), ("p", ctypes.c_double)]
+                ("order", I32), ("num_temps", I32), ("p", ctypes.c_double),
+                ("max_samples", I32), ("pad_", I32)]
 
 
 _lib = None

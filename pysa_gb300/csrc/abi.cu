@@ -566,8 +566,8 @@ int pysa_gb_ais(const pysa_gb_problems* p, pysa_gb_state* s,
                 const float* temps, double* log_w, void* stream) {
   if (!p || !s || !ws || !o || !temps || !log_w || !ws->fields)
     return fail(PYSA_GB_ERR_ARG, "ais: null argument");
-  if (p->num_instances != 1)
-    return fail(PYSA_GB_ERR_ARG, "ais: exactly one instance");
+  if (p->num_instances < 1)
+    return fail(PYSA_GB_ERR_ARG, "ais: no instance");
   if (p->max_n > 1024) return fail(PYSA_GB_ERR_SIZE, "ais: n > 1024");
   if (o->num_temps < 0) return fail(PYSA_GB_ERR_ARG, "ais: num_temps < 0");
   if (o->update == PYSA_GB_RANDOM &&
@@ -575,45 +575,45 @@ int pysa_gb_ais(const pysa_gb_problems* p, pysa_gb_state* s,
     return fail(PYSA_GB_ERR_ARG, "ais: perm workspace needs num_temps slots");
   if (o->reference == 1 && !(o->p > 0.0 && o->p < 1.0))
     return fail(PYSA_GB_ERR_ARG, "ais: bernoulli p must be in (0, 1)");
+  if (o->max_samples < 0) return fail(PYSA_GB_ERR_ARG, "ais: max_samples < 0");
   cudaStream_t st = (cudaStream_t)stream;
-  int32_t n = 0, ld = 0;
-  int64_t j_off = 0;
-  cudaError_t e = cudaMemcpyAsync(&n, p->n, sizeof(n), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&ld, p->ld, sizeof(ld), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&j_off, p->j_off, sizeof(j_off), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return cuda_fail(e, "ais: read instance");
+  cudaError_t e;
   if (o->update == PYSA_GB_RANDOM) {
-    e = launch_perm_range(n, p->max_n, 0u, 0u, o->num_temps, o->seed, ws->perm,
-                          st);
+    e = launch_perm_all(p->n, p->num_instances, p->max_n, o->num_temps,
+                        o->seed, ws->perm, st);
     if (e != cudaSuccess) return cuda_fail(e, "ais: orders");
   }
   AisArgs a;
   a.problem_type = p->problem_type;
-  a.n = n;
-  a.ld = ld;
   a.words = p->words;
   a.num_temps = o->num_temps;
   a.update = o->update;
   a.ref = o->reference;
   a.order = o->order;
-  a.inst = 0;
   a.max_n = p->max_n;
-  a.samples = p->num_chains;
+  a.num_instances = p->num_instances;
   a.p = o->p;
   a.seed = o->seed;
-  a.J = p->J + j_off;
+  a.n_tab = p->n;
+  a.ld_tab = p->ld;
+  a.replicas = p->replicas;
+  a.reads = p->reads;
+  a.j_off = p->j_off;
+  a.chain_off = p->chain_off;
+  a.J = p->J;
   a.temps = temps;
   a.perm = ws->perm;
   a.fields = ws->fields;
   a.field_ld = ws->field_ld;
+  a.pad_ = 0;
   a.spins = s->spins;
   a.energies = s->energies;
   a.log_w = log_w;
-  if (a.samples > 0) {
-    e = launch_ais(a, st);
+  a.status = s->status;
+  const int64_t max_samples =
+      o->max_samples > 0 ? o->max_samples : p->num_chains;
+  if (max_samples > 0) {
+    e = launch_ais(a, max_samples, st);
     if (e != cudaSuccess) return cuda_fail(e, "ais launch");
   }
   return PYSA_GB_OK;

@@ -22,9 +22,18 @@ template <int NC, int GW>
 __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const int n = a.n;
+  const int inst = blockIdx.y;
+  if (a.replicas[inst] != 1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_status(a.status, PYSA_GB_ERR_ARG);
+    return;
+  }
+  const int n = a.n_tab[inst];
+  const int ld = a.ld_tab[inst];
+  const int64_t samples = a.reads[inst];
+  const int64_t cbase = a.chain_off[inst];
+  const float* Jp = a.J + a.j_off[inst];
   const int64_t s0 = (int64_t)warp * GW;
-  if (s0 >= a.samples) return;
+  if (s0 >= samples) return;
   const bool ising = a.problem_type == PYSA_GB_ISING;
   const int words = (n + 31) >> 5;
 
@@ -33,21 +42,24 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
 #pragma unroll
   for (int g = 0; g < GW; ++g) {
     const int64_t smp = s0 + g;
-    const bool valid = smp < a.samples;
+    const bool valid = smp < samples;
 #pragma unroll
     for (int m = 0; m < NC; ++m) {
       const int col = 32 * m + lane;
-      H[g][m] = (valid && col < n) ? a.fields[smp * a.field_ld + col] : 0.0f;
-      spin[g][m] = (valid && m < words) ? a.spins[smp * a.words + m] : 0u;
+      H[g][m] = (valid && col < n)
+                    ? a.fields[(cbase + smp) * a.field_ld + col] : 0.0f;
+      spin[g][m] =
+          (valid && m < words) ? a.spins[(cbase + smp) * a.words + m] : 0u;
     }
   }
   const int gl = lane < GW ? lane : 0;
-  const bool lane_valid = lane < GW && s0 + lane < a.samples;
-  const int64_t my = s0 + gl;
-  double E = lane_valid ? (double)a.energies[my] : 0.0;
+  const bool lane_valid = lane < GW && s0 + lane < samples;
+  const int64_t my = s0 + gl;         // sample index within the instance
+  const int64_t myc = cbase + my;     // its chain
+  double E = lane_valid ? (double)a.energies[myc] : 0.0;
   int ones = 0;  // bits at 1 (spin +1 / x = 1) of lane g's sample
   if (lane_valid)
-    for (int w = 0; w < words; ++w) ones += __popc(a.spins[my * a.words + w]);
+    for (int w = 0; w < words; ++w) ones += __popc(a.spins[myc * a.words + w]);
   double lw = 0.0;
   float beta_old = 0.0f;
   const double lr = a.ref == 1 ? log((1.0 - a.p) / a.p) : 0.0;
@@ -63,7 +75,8 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
       lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
             ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
     }
-    const int32_t* perm = a.perm + (int64_t)k * a.max_n;
+    const int32_t* perm =
+        a.perm + ((int64_t)k * a.num_instances + inst) * a.max_n;
     for (int t = 0; t < n; ++t) {
       const int i = a.update == PYSA_GB_RANDOM ? perm[t] : t;
       const int m = i >> 5, l = i & 31;
@@ -90,7 +103,7 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
       const double refd = sbit ? -lr : lr;  // bit going down : up
       bool acc = false;
       if (lane_valid) {
-        const uint32_t x = draw1(a.seed, TAG_AIS, (uint32_t)a.inst, (uint32_t)k,
+        const uint32_t x = draw1(a.seed, TAG_AIS, (uint32_t)inst, (uint32_t)k,
                                  (uint32_t)my, (uint32_t)t);
         const double full = (double)beta * (double)dn + (1.0 - (double)beta) * refd;
         acc = accept_full(full, x);
@@ -102,7 +115,7 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
         ones += sbit ? -1 : 1;
       }
       if (am) {
-        const float* row = a.J + (int64_t)i * a.ld;
+        const float* row = Jp + (int64_t)i * ld;
         float Jr[NC];
 #pragma unroll
         for (int mm = 0; mm < NC; ++mm) {
@@ -133,16 +146,17 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
     beta_old = beta;
   }
   if (lane_valid) {
-    a.log_w[my] = lw;
-    a.energies[my] = (float)E;
+    a.log_w[myc] = lw;
+    a.energies[myc] = (float)E;
   }
 #pragma unroll
   for (int g = 0; g < GW; ++g) {
     const int64_t smp = s0 + g;
-    if (smp < a.samples) {
+    if (smp < samples) {
 #pragma unroll
       for (int m = 0; m < NC; ++m)
-        if (m < words && lane == 0) a.spins[smp * a.words + m] = spin[g][m];
+        if (m < words && lane == 0)
+          a.spins[(cbase + smp) * a.words + m] = spin[g][m];
     }
   }
 }
@@ -150,34 +164,39 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
 // Warp per sample keeps the code simple for the small n AIS is used on;
 // GW samples per warp amortise the decision shuffles.
 template <int NC, int GW>
-static cudaError_t launch_ais_t(const AisArgs& a, cudaStream_t st) {
-  const int64_t warps = (a.samples + GW - 1) / GW;
+static cudaError_t launch_ais_t(const AisArgs& a, int64_t max_samples,
+                                cudaStream_t st) {
+  const int64_t warps = (max_samples + GW - 1) / GW;
   const int64_t blocks = (warps * 32 + 127) / 128;
-  k_ais<NC, GW><<<(unsigned)blocks, 128, 0, st>>>(a);
+  dim3 grid((unsigned)(blocks > 0 ? blocks : 1), (unsigned)a.num_instances);
+  k_ais<NC, GW><<<grid, 128, 0, st>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ais(const AisArgs& a, cudaStream_t st) {
-  const int nc = (a.n + 31) / 32;
-  if (nc <= 1) return launch_ais_t<1, 8>(a, st);
-  if (nc <= 2) return launch_ais_t<2, 8>(a, st);
-  if (nc <= 4) return launch_ais_t<4, 8>(a, st);
-  if (nc <= 8) return launch_ais_t<8, 4>(a, st);
-  if (nc <= 16) return launch_ais_t<16, 2>(a, st);
-  if (nc <= 32) return launch_ais_t<32, 1>(a, st);
+cudaError_t launch_ais(const AisArgs& a, int64_t max_samples, cudaStream_t st) {
+  const int nc = (a.max_n + 31) / 32;
+  if (nc <= 1) return launch_ais_t<1, 8>(a, max_samples, st);
+  if (nc <= 2) return launch_ais_t<2, 8>(a, max_samples, st);
+  if (nc <= 4) return launch_ais_t<4, 8>(a, max_samples, st);
+  if (nc <= 8) return launch_ais_t<8, 4>(a, max_samples, st);
+  if (nc <= 16) return launch_ais_t<16, 2>(a, max_samples, st);
+  if (nc <= 32) return launch_ais_t<32, 1>(a, max_samples, st);
   return cudaErrorInvalidValue;
 }
 
-// Visiting orders for explicit sweep indices first..first+count-1.
-__global__ void k_perm_range(int n, int max_n, uint32_t inst, uint32_t first,
-                             uint64_t seed, int32_t* out) {
+// Fisher-Yates of instance blockIdx.y for sweep blockIdx.x (draws of
+// stream PERM, a = sweep), j = floor(x (i+1) / 2^32).
+__global__ void k_perm_all(const int32_t* n_tab, int num_instances, int max_n,
+                           uint64_t seed, int32_t* out) {
   extern __shared__ int32_t sh[];
-  const uint32_t sweep = first + blockIdx.x;
+  const int inst = blockIdx.y;
+  const int n = n_tab[inst];
+  const uint32_t sweep = blockIdx.x;
   int32_t* p = sh;
   uint32_t* x = reinterpret_cast<uint32_t*>(sh + max_n);
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     p[i] = i;
-    x[i] = draw1(seed, TAG_PERM, inst, sweep, 0u, (uint32_t)i);
+    x[i] = draw1(seed, TAG_PERM, (uint32_t)inst, sweep, 0u, (uint32_t)i);
   }
   __syncthreads();
   if (threadIdx.x == 0)
@@ -188,16 +207,17 @@ __global__ void k_perm_range(int n, int max_n, uint32_t inst, uint32_t first,
       p[j] = t;
     }
   __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x)
-    out[(int64_t)blockIdx.x * max_n + i] = p[i];
+  int32_t* o = out + ((int64_t)sweep * num_instances + inst) * max_n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) o[i] = p[i];
 }
 
-cudaError_t launch_perm_range(int n, int max_n, uint32_t inst, uint32_t first,
-                              int count, uint64_t seed, int32_t* out,
-                              cudaStream_t st) {
-  if (count <= 0) return cudaSuccess;
-  k_perm_range<<<count, 256, sizeof(int32_t) * 2 * max_n, st>>>(
-      n, max_n, inst, first, seed, out);
+cudaError_t launch_perm_all(const int32_t* n_tab, int num_instances, int max_n,
+                            int count, uint64_t seed, int32_t* out,
+                            cudaStream_t st) {
+  if (count <= 0 || num_instances <= 0) return cudaSuccess;
+  dim3 grid((unsigned)count, (unsigned)num_instances);
+  k_perm_all<<<grid, 256, sizeof(int32_t) * 2 * max_n, st>>>(
+      n_tab, num_instances, max_n, seed, out);
   return cudaGetLastError();
 }
 

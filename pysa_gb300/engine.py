@@ -398,31 +398,58 @@ def run_ais(problem_type: str, J: np.ndarray, h: np.ndarray,
     J, h already scaled by the target beta; init_states [Ns, n] (+-1 or
     0/1).  Returns (samples [Ns, n] float32, log weights [Ns] float64).
     """
-    ns, n = init_states.shape
+    return run_ais_batch(problem_type, [(J, h, init_states)], temps,
+                         seed=seed, update=update, reference=reference, p=p,
+                         order=order)[0]
+
+
+def run_ais_batch(problem_type: str, instances: list, temps: np.ndarray, *,
+                  seed: int, update: str = "sequential",
+                  reference: str = "uniform", p: float = 0.5,
+                  order: str = "reference"):
+    """AIS of many instances in one launch on one temperature schedule.
+
+    instances: [(J, h, init_states [Ns_i, n_i])], couplings already scaled
+    by the target beta.  Instance i uses the random streams of instance
+    index i, so a one-instance call gives the same result as index 0 of a
+    batch.  Returns [(samples [Ns_i, n_i] float32, log weights [Ns_i])].
+    """
     temps = np.asarray(temps, np.float32)
-    batch = PTBatch(problem_type, [Instance(np.asarray(J, np.float32),
-                                            np.asarray(h, np.float32),
-                                            np.ones(1, np.float32), ns)],
-                    perm_slots=max(len(temps), 1), kernel="plain")
-    batch.set_states(pack_spins(init_states.reshape(ns, 1, n), problem_type,
-                                batch.words), None)
+    insts = [Instance(np.asarray(J, np.float32), np.asarray(h, np.float32),
+                      np.ones(1, np.float32), int(x0.shape[0]))
+             for J, h, x0 in instances]
+    batch = PTBatch(problem_type, insts, perm_slots=max(len(temps), 1),
+                    kernel="plain")
+    words = batch.words
+    batch.set_states(np.concatenate([
+        pack_spins(np.asarray(x0).reshape(x0.shape[0], 1, -1), problem_type,
+                   words).reshape(-1, words) for _, _, x0 in instances]),
+        None)
     temps_d = torch.from_numpy(temps).to(batch.device)
-    log_w = torch.zeros(max(ns, 1), dtype=torch.float64, device=batch.device)
+    C = max(batch.num_chains, 1)
+    log_w = torch.zeros(C, dtype=torch.float64, device=batch.device)
+    max_samples = max(int(x0.shape[0]) for _, _, x0 in instances)
     opts = _lib.AisOptions(int(seed) & ((1 << 64) - 1),
                            _lib.RANDOM if update == "random" else
                            _lib.SEQUENTIAL,
                            0 if reference == "uniform" else 1,
                            0 if order == "reference" else 1, len(temps),
-                           float(p))
+                           float(p), max_samples, 0)
     check(batch.lib.pysa_gb_ais(ref(batch.p), ref(batch.s), ref(batch.ws),
                                 ref(opts), temps_d.data_ptr(),
                                 log_w.data_ptr(), batch._stream.cuda_stream),
           "ais")
     torch.cuda.synchronize(batch.device)
     batch.check_status()
-    samples = unpack_spins(batch.spins.cpu().numpy().view("<u4")[:ns], n,
-                           problem_type, np.float32)
-    return samples, log_w.cpu().numpy()[:ns]
+    spins = batch.spins.cpu().numpy().view("<u4")
+    lw = log_w.cpu().numpy()
+    out = []
+    for i, (_, _, x0) in enumerate(instances):
+        ns, n = x0.shape
+        c0 = int(batch.chain_off[i])
+        out.append((unpack_spins(spins[c0:c0 + ns], n, problem_type,
+                                 np.float32), lw[c0:c0 + ns]))
+    return out
 
 
 def logz_exact(problem_type: str, instances: list, beta: float = 1.0):

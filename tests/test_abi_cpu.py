@@ -30,7 +30,7 @@ def test_struct_sizes_match_header_layout():
     assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 14 * 8
     assert ctypes.sizeof(_lib.State) == 11 * 8
     assert ctypes.sizeof(_lib.Options) == 8 + 6 * 4
-    assert ctypes.sizeof(_lib.AisOptions) == 8 + 4 * 4 + 8
+    assert ctypes.sizeof(_lib.AisOptions) == 8 + 4 * 4 + 8 + 2 * 4
 
 
 def _tables(n, R, Rd):

@@ -69,3 +69,28 @@ def test_ais_estimate_vs_exact_n24():
     # within the sampling error of 1024 samples
     assert max(abs(e) for e in errs_std) < 0.15, errs_std
     assert min(errs_ref) > -0.1 and np.mean(errs_ref) > np.mean(errs_std)
+
+
+@pytest.mark.parametrize("update", ["sequential", "random"])
+def test_batched_ais_matches_oracle_per_instance(oracle, update):
+    """Several instances of different n and sample counts in one launch:
+    each instance i follows the oracle's ais_run with instance index i (its
+    own random streams), bit for bit on integer couplings."""
+    from pysa_gb300.engine import run_ais_batch
+    rng = np.random.default_rng(9)
+    insts = []
+    for n, ns in ((12, 40), (33, 17), (7, 64)):
+        J = np.triu(rng.integers(-2, 3, (n, n)), 1)
+        J = (J + J.T).astype(np.float32)
+        h = rng.integers(-1, 2, n).astype(np.float32)
+        x0 = (2 * rng.integers(0, 2, (ns, n)) - 1).astype(np.float32)
+        insts.append((0.5 * J, 0.5 * h, x0))
+    temps = np.linspace(0.05, 1.0, 15).astype(np.float32)
+    got = run_ais_batch("ising", insts, temps, seed=1234, update=update,
+                        reference="bernoulli", p=0.3)
+    for i, ((J, h, x0), (samples, lw)) in enumerate(zip(insts, got)):
+        want_s, want_lw = oracle.ais_run("ising", J, h, temps, x0, seed=1234,
+                                         update=update, ref="bernoulli",
+                                         p=0.3, inst=i)
+        assert np.array_equal(samples, want_s), f"instance {i}"
+        np.testing.assert_allclose(lw, want_lw, rtol=1e-9, atol=1e-9)
