@@ -683,7 +683,9 @@ def main():
         batch.set_states(pack_spins(
             np.zeros((Rd, R, n), np.float32), ptype, batch.words), None)
         batch.autotune()
-    use_tc = batch.tc and w["update"] == "sequential"
+    use_tc = batch.tc
+    if use_tc and w["update"] == "random":
+        batch._setup_random_tc()   # tiles repacked in each sweep's order
     rng = np.random.default_rng(100 + rank)
     if ptype == "qubo":
         x0 = rng.integers(0, 2, (Rd, R, n)).astype(np.float32)
@@ -882,7 +884,7 @@ def main():
                        "reads": Rd, "chains": C, "update": w["update"],
                        "exchange": "every sweep", "problem": w["kind"],
                        "l2": ("flushed (256 MB write) before every timed "
-                              "launch of %d sweeps; fields stay in tensor "
+                              "call of %d sweeps; fields stay in tensor "
                               "memory within a launch" % chunk) if fused else
                              "flushed (256 MB write) before every step",
                        "sweeps_per_launch": chunk,

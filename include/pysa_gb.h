@@ -144,6 +144,17 @@ typedef struct {
                                persistent tensor-core kernel */
   int32_t tc_unit_sweeps;   /* sweeps per work unit of that kernel (0: 8) */
   int32_t tc_launch_sweeps; /* most sweeps one launch of it covers (0: 64) */
+  /* random visiting order on the tensor cores: J tiles and diagonal blocks
+   * repacked in each sweep's order, tc_rand_slots sweeps at a time (0: random
+   * sweeps run on the plain kernel); needs perm_slots >= tc_rand_slots */
+  uint16_t *tc_b_rand;      /* [tc_rand_slots, tc_b_elems] */
+  float *tc_diag_rand;      /* [tc_rand_slots, tc_diag_elems] */
+  int64_t *tc_inst_off;     /* [2 * num_instances] device, written by
+                               pysa_gb_tc_setup when not NULL: offsets of each
+                               instance's tiles and diagonal blocks, -1 for
+                               plain-kernel instances */
+  int32_t tc_rand_slots;
+  int32_t pad_;
 } pysa_gb_workspace;
 
 /* Host copies of the per-instance tables, used to plan the work list. */

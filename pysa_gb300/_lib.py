@@ -47,7 +47,9 @@ class Workspace(ctypes.Structure):
                 ("tc_variant_start", I32 * 3), ("tc_variant_count", I32 * 3),
                 ("tc_min_n", I32), ("tc_inst", P), ("plain_live", I32),
                 ("tc_fusable", I32), ("tc_sched", P), ("tc_unit_sweeps", I32),
-                ("tc_launch_sweeps", I32)]
+                ("tc_launch_sweeps", I32), ("tc_b_rand", P),
+                ("tc_diag_rand", P), ("tc_inst_off", P),
+                ("tc_rand_slots", I32), ("pad_", I32)]
 
 
 class HostTables(ctypes.Structure):

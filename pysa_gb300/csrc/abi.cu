@@ -371,6 +371,18 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
                                    ws->tc_diag + doff[i], st);
     if (e != cudaSuccess) return cuda_fail(e, "pack tc tiles");
   }
+  if (ws->tc_inst_off && p->num_instances > 0) {
+    std::vector<int64_t> off(2 * (size_t)p->num_instances, -1);
+    for (int i = 0; i < p->num_instances; ++i)
+      if (flags[i]) {
+        off[2 * i] = boff[i];
+        off[2 * i + 1] = doff[i];
+      }
+    cudaError_t e = cudaMemcpyAsync(ws->tc_inst_off, off.data(),
+                                    off.size() * sizeof(int64_t),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy tc instance offsets");
+  }
   // host vectors above are pageable: the copies are complete on return
   ws->plain_live = live;
   ws->tc_fusable = fusable;
@@ -414,7 +426,12 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
                 "base 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   int caps[kNumPlainVariants];
-  const bool tc_path = ws->tc_enabled && !random && ws->tc_items;
+  // random order on the tensor cores needs the repacked-tile slots and as
+  // many visiting-order slots
+  const bool rand_tc = random && ws->tc_rand_slots > 0 && ws->tc_b_rand &&
+                       ws->tc_diag_rand && ws->tc_inst_off &&
+                       ws->perm_slots >= ws->tc_rand_slots;
+  const bool tc_path = ws->tc_enabled && ws->tc_items && (!random || rand_tc);
   // plain variants that run: all of them, or (tensor-core path) those with
   // instances left to the plain kernel
   const int plain_mask = tc_path ? ws->plain_live : 0xFF;
@@ -449,7 +466,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   pa.perm_slots = a.perm_slots;
   pa.seed = o->seed;
   const int phases = o->phases ? o->phases : 3;
-  const bool use_tc = ws->tc_enabled && !random && ws->tc_items;
+  const bool use_tc = tc_path;
   TcArgs ta;
   ta.p = *p;
   ta.s = *s;
@@ -463,6 +480,13 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.use_pt = o->use_pt;
   ta.pad_ = 0;
   ta.sched = ws->tc_sched;
+  ta.perm = ws->perm;
+  ta.perm_slots = a.perm_slots;
+  ta.rand_slots = ws->tc_rand_slots;
+  ta.rand_b = ws->tc_b_rand;
+  ta.rand_diag = ws->tc_diag_rand;
+  ta.rand_b_stride = ws->tc_b_elems;
+  ta.rand_diag_stride = ws->tc_diag_elems;
   ta.trace = g_tc_trace;
   const int sms = sm_count();
   const int folds[3] = {1, 2, 4};
@@ -485,7 +509,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
       ta.units_per_item = units;
       ta.fuse_exchange = fuse;
       ta.advance_counter = fuse && v == last_v;
-      e = launch_tc(ta, folds[v], sms, st);
+      e = launch_tc(ta, folds[v], random, sms, st);
       if (e != cudaSuccess) return cuda_fail(e, "tc sweep launch");
     }
     return PYSA_GB_OK;
@@ -496,15 +520,31 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   const bool fused = use_tc && phases == 3 && ws->plain_live == 0 &&
                      o->log_omega_stride == 0 &&
                      (!o->use_pt || ws->tc_fusable) && ws->tc_sched;
+  // random order on the tensor cores: visiting orders of the next `cnt`
+  // sweeps, and the tiles repacked in those orders
+  auto rand_prepare = [&](int cnt) -> int {
+    launch_perm(pa, st, cnt);
+    cudaError_t e = launch_repack_tc(
+        *p, ws->tc_terms, ws->tc_inst_off, ws->perm, a.perm_slots,
+        s->sweep_counter, cnt, ws->tc_rand_slots, ws->tc_b_rand,
+        ws->tc_b_elems, ws->tc_diag_rand, ws->tc_diag_elems, st);
+    return e == cudaSuccess ? PYSA_GB_OK : cuda_fail(e, "tc repack");
+  };
   if (fused) {
     const int ku_pref = ws->tc_unit_sweeps > 0 ? ws->tc_unit_sweeps : 8;
-    const int per_launch =
+    int per_launch =
         ws->tc_launch_sweeps > 0 ? ws->tc_launch_sweeps : kMaxFusedSweeps;
+    if (random && per_launch > ws->tc_rand_slots)
+      per_launch = ws->tc_rand_slots;
     int remaining = num_sweeps;
     while (remaining > 0) {
       int chunk = remaining < per_launch ? remaining : per_launch;
       const int ku = chunk < ku_pref ? chunk : ku_pref;
       chunk = chunk / ku * ku;
+      if (random) {
+        const int rc = rand_prepare(chunk);
+        if (rc != PYSA_GB_OK) return rc;
+      }
       const int rc = tc_launches(ku, chunk / ku, 1);
       if (rc != PYSA_GB_OK) return rc;
       remaining -= chunk;
@@ -513,6 +553,10 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   }
   for (int sw = 0; sw < num_sweeps; ++sw) {
     if (use_tc && (phases & 1)) {
+      if (random) {
+        const int rc = rand_prepare(1);
+        if (rc != PYSA_GB_OK) return rc;
+      }
       const int rc = tc_launches(1, 1, 0);
       if (rc != PYSA_GB_OK) return rc;
     }

@@ -37,7 +37,9 @@ void launch_pack_rows(const float* J, int ld, int n, int nc, int ls,
                       float* packed, cudaStream_t st);
 void launch_prepare(const PrepArgs& a, cudaStream_t st);
 void launch_exchange(const XArgs& a, cudaStream_t st);
-void launch_perm(const PermArgs& a, cudaStream_t st);
+// Visiting orders of the current sweep and the count - 1 after it (slots
+// sweep % perm_slots).
+void launch_perm(const PermArgs& a, cudaStream_t st, int count = 1);
 void launch_energy64(int ptype, int n, int ld, const double* J,
                      const double* h, const uint32_t* spins, int words,
                      int64_t count, double* out, cudaStream_t st);

@@ -214,7 +214,8 @@ __global__ void k_perm(const PermArgs a) {
   extern __shared__ int32_t sh[];
   const int inst = blockIdx.x;
   const int n = a.p.n[inst];
-  const uint32_t sweep = (uint32_t)(*a.sweep_counter);
+  // grid row y: the sweep y after the current one (orders made ahead)
+  const uint32_t sweep = (uint32_t)(*a.sweep_counter) + blockIdx.y;
   int32_t* p = sh;
   uint32_t* x = reinterpret_cast<uint32_t*>(sh + a.p.max_n);
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -236,9 +237,10 @@ __global__ void k_perm(const PermArgs a) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = p[i];
 }
 
-void launch_perm(const PermArgs& a, cudaStream_t st) {
+void launch_perm(const PermArgs& a, cudaStream_t st, int count) {
   const size_t sm = sizeof(int32_t) * 2 * (size_t)a.p.max_n;
-  k_perm<<<a.p.num_instances, 256, sm, st>>>(a);
+  dim3 grid((unsigned)a.p.num_instances, (unsigned)(count > 0 ? count : 1));
+  k_perm<<<grid, 256, sm, st>>>(a);
 }
 
 // ----------------------------------------------------------- f64 energy

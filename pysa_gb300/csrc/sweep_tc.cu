@@ -30,10 +30,12 @@
 
 namespace pysa_gb {
 
-template <int F>
+// RND: random visiting order (one permutation per instance and sweep); the
+// B ring keeps two stages to make room for the gathered block fields.
+template <int F, bool RND = false>
 struct TcCfg {
   static constexpr int CC = 128 / F;          // chains per CTA
-  static constexpr int NS = F == 1 ? 2 : 3;   // B ring stages
+  static constexpr int NS = (F == 1 || RND) ? 2 : 3;   // B ring stages
   static constexpr int WORDS = 16 * F;        // spin words per chain
   static constexpr size_t A_OFF = 0;
   static constexpr size_t A_BYTES = (size_t)F * 16384;
@@ -52,7 +54,19 @@ struct TcCfg {
   static constexpr bool HELP = F == 2;
   static constexpr size_t CORR_OFF = BETA_OFF + CC * 4;
   static constexpr size_t CORR_BYTES = HELP ? (size_t)2 * 16 * CC * 4 : 0;
-  static constexpr size_t BAR_OFF = (CORR_OFF + CORR_BYTES + 63) / 64 * 64;
+  // RND, F > 1: fields of the block's 64 scattered columns, gathered by the
+  // warps whose slices hold them ([64][CC] floats)
+  static constexpr size_t HBUF_OFF = CORR_OFF + CORR_BYTES;
+  static constexpr size_t HBUF_BYTES =
+      (RND && F > 1) ? (size_t)64 * CC * 4 : 0;
+  // RND: each decision warp's copy of the block's 64 permutation entries
+  static constexpr size_t PERM_OFF = HBUF_OFF + HBUF_BYTES;
+  static constexpr size_t PERM_BYTES = RND ? (size_t)4 * 64 * 4 : 0;
+  // RND: position-ordered spin words of the next blocks, [2][2][CC], made
+  // by the log-uniform helper warps
+  static constexpr size_t POSB_OFF = PERM_OFF + PERM_BYTES;
+  static constexpr size_t POSB_BYTES = RND ? (size_t)2 * 2 * CC * 4 : 0;
+  static constexpr size_t BAR_OFF = (POSB_OFF + POSB_BYTES + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
   // lf_full[2], lf_free[2], full[NS], free[NS]
   static constexpr int NBARS = 13 + 2 * NS;
@@ -125,9 +139,9 @@ __device__ __forceinline__ uint32_t bf16_bits(float d) {
 // previous unit is done, which a CTA that is already running owns, so the
 // wait always ends.  Within a unit the fields stay in TMEM across sweeps; the
 // replica exchange of the item's reads runs in the kernel when fused.
-template <int F>
+template <int F, bool RND>
 __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
-  using C = TcCfg<F>;
+  using C = TcCfg<F, RND>;
   constexpr int CC = C::CC;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::BAR_OFF);
@@ -156,6 +170,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
   float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
   float* corr_s = reinterpret_cast<float*>(smem + C::CORR_OFF);
+  float* hbuf = reinterpret_cast<float*>(smem + C::HBUF_OFF);
+  int32_t* perm_s = reinterpret_cast<int32_t*>(smem + C::PERM_OFF);
+  uint32_t* posb = reinterpret_cast<uint32_t*>(smem + C::POSB_OFF);
   // exchange scratch between sweeps (dl_s is idle then): energies [CC],
   // per warp slot->replica, uniforms, their logs and the betas [4][CC] each
   float* ex_E = dl_s;
@@ -417,15 +434,76 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 
         // ============================================================ decide
         const float beta = beta_s[c];
+        // random order: this sweep's permutation (position -> spin)
+        const int32_t* pi_row =
+            RND ? a.perm + ((int64_t)(sweep % (uint32_t)a.perm_slots) *
+                                a.p.num_instances + inst) * a.p.max_n
+                : nullptr;
         for (int t = 0; t < NB; ++t) {
           const uint32_t Gb = Gs + (uint32_t)t;
           const int i0 = 64 * t;
-          const int qt = i0 / S, co = i0 % S;
+          // deciding slice: the one holding the block's columns, or slice 0
+          // in random order (columns scattered over all slices)
+          const int qt = RND ? 0 : i0 / S, co = i0 % S;
           const int kmax = n - i0 < 64 ? n - i0 : 64;
+          const bool wait_h = Gb > G0 && !(t == 0 && rc_at(s));
+          // random order: lane l holds the spins at positions l and 32 + l
+          // of this block (-1 past the end) with their slice and column;
+          // everything else reads them by warp shuffle
+          int pk0 = -1, pk1 = -1, ps0 = -1, ps1 = -1, pc0 = 0, pc1 = 0;
+          if constexpr (RND) {
+            if (warp < 4) {
+              if (lane < kmax) pk0 = pi_row[i0 + lane];
+              if (32 + lane < kmax) pk1 = pi_row[i0 + 32 + lane];
+              if (pk0 >= 0) { ps0 = pk0 / S; pc0 = pk0 - ps0 * S; }
+              if (pk1 >= 0) { ps1 = pk1 / S; pc1 = pk1 - ps1 * S; }
+              perm_s[warp * 64 + lane] = pk0;
+              perm_s[warp * 64 + 32 + lane] = pk1;
+              __syncwarp();
+            }
+          }
+          // spin at position k of this block (-1 past the end), from this
+          // warp's copy (same address in every lane: a broadcast load)
+          auto spos = [&](int k) { return perm_s[warp * 64 + k]; };
+          if constexpr (RND && F > 1) {
+            // every decision warp copies the block's fields held in its own
+            // slice (TMEM lanes belong to warps) into hbuf[k][chain]
+            bool hok = !*sh.abort;
+            if (hok && wait_h)
+              hok = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
+            hok = __all_sync(0xffffffffu, hok);
+            if (hok) {
+              tc::fence_after_sync();
+              for (int k0 = 0; k0 < 64; k0 += 16) {
+                uint32_t r[16];
+                int mine = 0;  // bit kk: position k0 + kk lives in my slice
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk) {
+                  const int k = k0 + kk;
+                  const int sl =
+                      __shfl_sync(0xffffffffu, k < 32 ? ps0 : ps1, k & 31);
+                  const int col =
+                      __shfl_sync(0xffffffffu, k < 32 ? pc0 : pc1, k & 31);
+                  r[kk] = 0u;
+                  if (sl == q) {
+                    r[kk] = tc::tmem_ld1_nowait(taddr + lane_base +
+                                                (uint32_t)col);
+                    mine |= 1 << kk;
+                  }
+                }
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk)
+                  if ((mine >> kk) & 1)
+                    hbuf[(k0 + kk) * CC + c] = __uint_as_float(r[kk]);
+              }
+            }
+            named_sync_128();
+          }
           bool go = q == qt && !*sh.abort;
           // fields of this block: the previous block's critical MMA (not
           // needed for a unit's first block or after a recompute)
-          if (go && Gb > G0 && !(t == 0 && rc_at(s)))
+          if (go && wait_h && !(RND && F > 1))
             go = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
           if (go) go = tc_wait(&sh.jbb_full[Gb & 1], (Gb >> 1) & 1, sh, status);
           if (go) go = tc_wait(&sh.lf_full[Gb & 1], (Gb >> 1) & 1, sh, status);
@@ -439,8 +517,16 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             if (lead) stamp(a, Gb, 1);
             const float* jb = jbb + (Gb & 1) * 4096;
             const float* lfb = lf_s + (Gb & 1) * 64 * CC;
-            const uint32_t o0 = spins_s[(2 * t) * CC + c];
-            const uint32_t o1 = spins_s[(2 * t + 1) * CC + c];
+            uint32_t o0 = 0u, o1 = 0u;
+            if constexpr (RND) {
+              // bit k of (o0, o1): spin at position k of the block, made by
+              // the helper warps with this block's log-uniforms
+              o0 = posb[((Gb & 1) * 2 + 0) * CC + c];
+              o1 = posb[((Gb & 1) * 2 + 1) * CC + c];
+            } else {
+              o0 = spins_s[(2 * t) * CC + c];
+              o1 = spins_s[(2 * t + 1) * CC + c];
+            }
             uint32_t w0 = o0, w1 = o1;
             float dEb = 0.0f;
             bool a_ok = true;
@@ -449,7 +535,27 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     #pragma unroll 1
             for (int g = 0; g < 4; ++g) {
               float hs[16];
-              tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
+              if constexpr (!RND) {
+                tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
+              } else if constexpr (F > 1) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                  hs[j] = 16 * g + j < kmax ? hbuf[(16 * g + j) * CC + c]
+                                            : 0.0f;
+              } else {
+                uint32_t r[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  const int sp = spos(16 * g + j);
+                  r[j] = 0u;
+                  if (sp >= 0)
+                    r[j] = tc::tmem_ld1_nowait(taddr + lane_base +
+                                               (uint32_t)sp);
+                }
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int j = 0; j < 16; ++j) hs[j] = __uint_as_float(r[j]);
+              }
               if (lead) stamp(a, Gb, 8 + 3 * g);
               // with helpers, sub-blocks older than g-1 arrive precomputed
               const int k_lo = (C::HELP && g >= 2) ? 16 * (g - 1) : 0;
@@ -475,6 +581,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               if (lead) stamp(a, Gb, 9 + 3 * g);
               uint32_t wcur = g < 2 ? w0 : w1;
               const int sb = 16 * (g & 1);
+
               // fast pass: branch-free decisions from the precomputed log-uniform;
               // a decision inside the f32 error band is only flagged here
               const uint32_t wsave = wcur;
@@ -590,8 +697,25 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
             }
             if (valid) {
-              spins_s[(2 * t) * CC + c] = w0;
-              spins_s[(2 * t + 1) * CC + c] = w1;
+              if constexpr (!RND) {
+                spins_s[(2 * t) * CC + c] = w0;
+                spins_s[(2 * t + 1) * CC + c] = w1;
+              } else {
+                // flips back to the scattered spins
+                uint32_t f0 = w0 ^ o0, f1 = w1 ^ o1;
+                while (f0) {
+                  const int k = __ffs(f0) - 1;
+                  f0 &= f0 - 1;
+                  const int sp = spos(k);
+                  spins_s[(sp >> 5) * CC + c] ^= 1u << (sp & 31);
+                }
+                while (f1) {
+                  const int k = __ffs(f1) - 1;
+                  f1 &= f1 - 1;
+                  const int sp = spos(32 + k);
+                  spins_s[(sp >> 5) * CC + c] ^= 1u << (sp & 31);
+                }
+              }
               dE_s[c] += (double)dEb;
             }
             fence_proxy_async();
@@ -841,7 +965,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               // issues the same order)
               for (int k = 0; k < F && ok; ++k) {
                 const int qq = (qn + k) % F;
-                const bool crit = jj == 0 && k == 0 && has_next;
+                // random order: the next block's columns are scattered, so
+                // no tile is critical; h_ready follows the whole block
+                const bool crit = !RND && jj == 0 && k == 0 && has_next;
                 for (int term = 0; term < T; ++term) {
                   const uint32_t slot = (u + term) % C::NS;
                   if (!tc_wait(&sh.full[slot], ((u + term) / C::NS) & 1, sh,
@@ -872,7 +998,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
             }
             if (!ok) break;
-            if (!has_next) tc::commit(sh.h_ready);  // one phase per block
+            if (!has_next || RND) {
+              tc::commit(sh.h_ready);  // one phase per block
+              if (RND) stamp(a, Gb, 6);
+            }
             tc::commit(sh.mma_done);
           }
         }
@@ -886,18 +1015,28 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
         const size_t tile_elems = 256 * 64;
         // diagonal block of global block Gx (block (Gx - G0) % NB of the
         // unit) into buffer Gx & 1, once block Gx - 2 has released it
+        // random order: the sweep's repacked slot (same offsets)
+        auto rand_slot = [&](int s_) {
+          return (int64_t)((sweep_first + (uint32_t)s_) %
+                           (uint32_t)(a.rand_slots > 0 ? a.rand_slots : 1));
+        };
         auto issue_jbb = [&](uint32_t Gx) {
           if (Gx >= 2 &&
               !tc_wait(&sh.jbb_free[Gx & 1], ((Gx >> 1) - 1) & 1, sh, status))
             return false;
           const int tx = (int)((Gx - G0) % (uint32_t)NB);
+          const float* Dx = D;
+          if (RND)
+            Dx = a.rand_diag + rand_slot((int)((Gx - G0) / (uint32_t)NB)) *
+                                   a.rand_diag_stride + item.diag_off;
           uint64_t* bar = &sh.jbb_full[Gx & 1];
           mbar_expect_tx_arrive(bar, 16384);
-          bulk_g2s(smem + C::JBB_OFF + (Gx & 1) * 16384, D + (size_t)tx * 4096,
+          bulk_g2s(smem + C::JBB_OFF + (Gx & 1) * 16384, Dx + (size_t)tx * 4096,
                    16384, bar);
           return true;
         };
-        auto issue_stage = [&](int t, int term, int qq, int j) {
+        auto issue_stage = [&](const uint16_t* Bsrc, int t, int term, int qq,
+                               int j) {
           const uint32_t slot = u % C::NS;
           if (u >= (uint32_t)C::NS &&
               !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh, status))
@@ -907,7 +1046,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
           const uint32_t bytes = (uint32_t)width * 128;
           mbar_expect_tx_arrive(&sh.full[slot], bytes);
-          bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, Bp + src, bytes,
+          bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, Bsrc + src, bytes,
                    &sh.full[slot]);
           ++u;
           return true;
@@ -919,8 +1058,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               for (int j = 0; j < NT && ok; ++j)
                 for (int term = 0; term < T && ok; ++term)
                   for (int qq = 0; qq < F && ok; ++qq)
-                    ok = issue_stage(t, term, qq, j);
+                    ok = issue_stage(Bp, t, term, qq, j);
           }
+          const uint16_t* Bs =
+              RND ? a.rand_b + rand_slot(s) * a.rand_b_stride + item.b_off
+                  : Bp;
           for (int t = 0; t < NB && ok; ++t) {
             const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
             // the next block's diagonal block lands while this one is decided
@@ -933,7 +1075,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
               for (int k = 0; k < F && ok; ++k)
                 for (int term = 0; term < T && ok; ++term)
-                  ok = issue_stage(t, term, (qn + k) % F, j);
+                  ok = issue_stage(Bs, t, term, (qn + k) % F, j);
             }
             stamp(a, Gb, 7);
           }
@@ -961,6 +1103,34 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
               for (int e = 0; e < 4; ++e)
                 out[(4 * quad + e) * CC + c2] = log_uniform_f32(x[e]);
+            }
+          }
+          if constexpr (RND) {
+            // spin words of this block in position order.  Its spins are
+            // not touched by earlier blocks of the same sweep; the previous
+            // sweep's last block must have finished (blocks Gb-2 and older
+            // have, by the lf_free wait above)
+            const uint32_t Gs = G0 + (uint32_t)(s * NB);
+            if (go && Gs > G0 && Gb - Gs <= 1)
+              go = tc_wait(&sh.lf_free[(Gs - 1) & 1], ((Gs - 1) >> 1) & 1, sh,
+                           status);
+            if (go) {
+              const int32_t* pr =
+                  a.perm + ((int64_t)(sweep % (uint32_t)a.perm_slots) *
+                                a.p.num_instances + inst) * a.p.max_n +
+                  64 * t;
+              const int kmax = n - 64 * t < 64 ? n - 64 * t : 64;
+              for (int c2 = hid; c2 < CC; c2 += 64) {
+                uint32_t w0 = 0u, w1 = 0u;
+                for (int k = 0; k < kmax; ++k) {
+                  const int sp = pr[k];
+                  const uint32_t bit =
+                      (spins_s[(sp >> 5) * CC + c2] >> (sp & 31)) & 1u;
+                  if (k < 32) w0 |= bit << k; else w1 |= bit << (k - 32);
+                }
+                posb[((Gb & 1) * 2 + 0) * CC + c2] = w0;
+                posb[((Gb & 1) * 2 + 1) * CC + c2] = w1;
+              }
             }
           }
           named_sync_helpers();
@@ -1048,6 +1218,83 @@ __global__ void k_pack_tc_diag(const float* Jt, int ld, int n, float* out) {
   }
 }
 
+// Random order: the same tiles and diagonal blocks with spin position
+// 64 t + k standing for spin perm[64 t + k] (rows of J^T gathered; field
+// columns stay natural in the tiles, both sides permuted in the diagonal
+// blocks).  Grid: x over elements, y = instance, z = sweep ahead.
+__global__ void k_repack_tc(const pysa_gb_problems p, int terms,
+                            const int64_t* inst_off, const int32_t* perm,
+                            int perm_slots, const int64_t* sweep_counter,
+                            int slots, uint16_t* b_out, int64_t b_stride,
+                            float* diag_out, int64_t diag_stride) {
+  const int inst = blockIdx.y;
+  const int64_t boff = inst_off[2 * inst], doff = inst_off[2 * inst + 1];
+  if (boff < 0) return;
+  const int n = p.n[inst], ld = p.ld[inst];
+  const float* Jt = p.J + p.j_off[inst];
+  const uint32_t sweep = (uint32_t)(*sweep_counter) + blockIdx.z;
+  const int32_t* pi =
+      perm + ((int64_t)(sweep % (uint32_t)perm_slots) * p.num_instances +
+              inst) * p.max_n;
+  const int64_t slot = sweep % (uint32_t)slots;
+  const int F = n <= 512 ? 1 : (n <= 1024 ? 2 : 4);
+  const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + 255) / 256;
+  const int64_t tile = 256 * 64;
+  const int64_t tb = (int64_t)NB * terms * F * NT * tile;
+  const int64_t td = (int64_t)NB * 4096;
+  uint16_t* bo = b_out + slot * b_stride + boff;
+  float* dout = diag_out + slot * diag_stride + doff;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tb + td;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < tb) {
+      int64_t rest = e;
+      const int within = (int)(rest % tile);
+      rest /= tile;
+      const int j = (int)(rest % NT);
+      rest /= NT;
+      const int qq = (int)(rest % F);
+      rest /= F;
+      const int term = (int)(rest % terms);
+      const int t = (int)(rest / terms);
+      const int cm = within / 64, inside = within % 64;
+      const int r = (cm / 8) * 8 + inside / 8;
+      const int k = (cm % 8) * 8 + inside % 8;
+      const int pos = 64 * t + k, col = qq * S + 256 * j + r;
+      float v = 0.0f;
+      if (pos < n && col < n && 256 * j + r < S)
+        v = Jt[(int64_t)pi[pos] * ld + col];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+      const __nv_bfloat16 o = term == 0 ? hi : lo;
+      bo[e] = *reinterpret_cast<const uint16_t*>(&o);
+    } else {
+      const int64_t d = e - tb;
+      const int t = (int)(d / 4096), k = (int)(d % 4096) / 64,
+                k2 = (int)(d % 64);
+      const int a1 = 64 * t + k, a2 = 64 * t + k2;
+      dout[d] = (a1 < n && a2 < n) ? Jt[(int64_t)pi[a1] * ld + pi[a2]] : 0.0f;
+    }
+  }
+}
+
+cudaError_t launch_repack_tc(const pysa_gb_problems& p, int terms,
+                             const int64_t* inst_off, const int32_t* perm,
+                             int perm_slots, const int64_t* sweep_counter,
+                             int count, int slots, uint16_t* b_out,
+                             int64_t b_stride, float* diag_out,
+                             int64_t diag_stride, cudaStream_t st) {
+  if (count <= 0 || p.num_instances <= 0) return cudaSuccess;
+  const int64_t per = tc_b_elems(p.max_n, terms) + tc_diag_elems(p.max_n);
+  int bx = (int)((per + 255) / 256);
+  if (bx > 1024) bx = 1024;
+  dim3 grid((unsigned)bx, (unsigned)p.num_instances, (unsigned)count);
+  k_repack_tc<<<grid, 256, 0, st>>>(p, terms, inst_off, perm, perm_slots,
+                                    sweep_counter, slots, b_out, b_stride,
+                                    diag_out, diag_stride);
+  return cudaGetLastError();
+}
+
 int tc_fold_for(int n) {
   if (n <= 512) return 1;
   if (n <= 1024) return 2;
@@ -1078,30 +1325,34 @@ cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
   return cudaGetLastError();
 }
 
-template <int F>
+template <int F, bool RND>
 static cudaError_t launch_tc_t(const TcArgs& a, int count, cudaStream_t st) {
   static bool attr_set[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !attr_set[dev]) {
     cudaError_t e = cudaFuncSetAttribute(
-        k_sweep_tc<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)TcCfg<F>::BYTES);
+        k_sweep_tc<F, RND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)TcCfg<F, RND>::BYTES);
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
-  k_sweep_tc<F><<<count, 256, TcCfg<F>::BYTES, st>>>(a);
+  k_sweep_tc<F, RND><<<count, 256, TcCfg<F, RND>::BYTES, st>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc(const TcArgs& a, int F, int max_ctas, cudaStream_t st) {
+cudaError_t launch_tc(const TcArgs& a, int F, bool random, int max_ctas,
+                      cudaStream_t st) {
   const int64_t units = (int64_t)a.num_items * a.units_per_item;
   if (units <= 0) return cudaSuccess;
   const int count = (int)(units < max_ctas ? units : max_ctas);
-  switch (F) {
-    case 1: return launch_tc_t<1>(a, count, st);
-    case 2: return launch_tc_t<2>(a, count, st);
-    case 4: return launch_tc_t<4>(a, count, st);
+  switch (F * 2 + (random ? 1 : 0)) {
+    case 2: return launch_tc_t<1, false>(a, count, st);
+    case 3: return launch_tc_t<1, true>(a, count, st);
+    case 4: return launch_tc_t<2, false>(a, count, st);
+    case 5: return launch_tc_t<2, true>(a, count, st);
+    case 8: return launch_tc_t<4, false>(a, count, st);
+    case 9: return launch_tc_t<4, true>(a, count, st);
   }
   return cudaErrorInvalidValue;
 }

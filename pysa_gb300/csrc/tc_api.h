@@ -34,6 +34,16 @@ struct TcArgs {
   int32_t pad_;
   int32_t* sched;  // zeroed per launch: [0] unit queue, [1] finished CTAs,
                    // [2 + item] units of the item done
+  // random order: permutation of (inst, sweep) at
+  // perm[((sweep % perm_slots) * num_instances + inst) * max_n]; tiles and
+  // diagonal blocks repacked in that order at slot sweep % rand_slots
+  const int32_t* perm;
+  int32_t perm_slots;
+  int32_t rand_slots;
+  const uint16_t* rand_b;
+  const float* rand_diag;
+  int64_t rand_b_stride;  // elements per slot
+  int64_t rand_diag_stride;
   // optional timeline of CTA 0 (globaltimer ns): [49][24] stamps
   unsigned long long* trace;
 };
@@ -46,6 +56,17 @@ cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
                            uint16_t* b_out, float* diag_out, cudaStream_t st);
 // Persistent launch over a.num_items * a.units_per_item work units with at
 // most `max_ctas` CTAs; a.sched must hold 2 + num_items zeroed words.
-cudaError_t launch_tc(const TcArgs& a, int F, int max_ctas, cudaStream_t st);
+// random: visiting order from a.perm, tiles from a.rand_b / a.rand_diag.
+cudaError_t launch_tc(const TcArgs& a, int F, bool random, int max_ctas,
+                      cudaStream_t st);
+// Tiles and diagonal blocks of every tensor-core instance (inst_off >= 0)
+// in the visiting order of the current sweep and the count - 1 after it,
+// into slot sweep % slots of b_out / diag_out.
+cudaError_t launch_repack_tc(const pysa_gb_problems& p, int terms,
+                             const int64_t* inst_off, const int32_t* perm,
+                             int perm_slots, const int64_t* sweep_counter,
+                             int count, int slots, uint16_t* b_out,
+                             int64_t b_stride, float* diag_out,
+                             int64_t diag_stride, cudaStream_t st);
 
 }  // namespace pysa_gb

@@ -80,6 +80,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// One column (32 lanes x 1) without waiting: the register is valid only
+// after tmem_wait_ld(); a warp gathers scattered columns with one wait.
+__device__ __forceinline__ uint32_t tmem_ld1_nowait(uint32_t taddr) {
+  uint32_t r;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];"
+               : "=r"(r)
+               : "r"(taddr)
+               : "memory");
+  return r;
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  __syncwarp();
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v) {
   __syncwarp();
   asm volatile(

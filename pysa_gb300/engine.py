@@ -228,6 +228,35 @@ class PTBatch:
         self.tc = True
         self.tc_min_n = int(min_n)
 
+    def _setup_random_tc(self, budget_bytes: int = 2 << 30,
+                         max_slots: int = 16):
+        """Buffers for random-order sweeps on the tensor cores: the tiles and
+        diagonal blocks repacked in each sweep's visiting order, for up to
+        `max_slots` sweeps at a time within `budget_bytes`, and as many
+        visiting-order slots.  Done once per batch."""
+        if self.ws.tc_rand_slots > 0:
+            return
+        per = 2 * int(self.ws.tc_b_elems) + 4 * int(self.ws.tc_diag_elems)
+        slots = int(max(1, min(max_slots, budget_bytes // max(per, 1))))
+        z = lambda k, dt: torch.zeros(k, dtype=dt, device=self.device)
+        I = len(self.instances)
+        self.tc_b_rand = z(max(slots * int(self.ws.tc_b_elems), 1),
+                           torch.int16)
+        self.tc_diag_rand = z(max(slots * int(self.ws.tc_diag_elems), 1),
+                              torch.float32)
+        self.tc_inst_off = z(2 * max(I, 1), torch.int64)
+        if self.perm_slots < slots:
+            self.perm_slots = slots
+            self.perm = z(self.perm_slots * I * self.max_n, torch.int32)
+            self.ws.perm = _ptr(self.perm)
+            self.ws.perm_slots = self.perm_slots
+        self.ws.tc_b_rand = _ptr(self.tc_b_rand)
+        self.ws.tc_diag_rand = _ptr(self.tc_diag_rand)
+        self.ws.tc_inst_off = _ptr(self.tc_inst_off)
+        # re-run the set-up so it writes the per-instance offsets
+        self._setup_tc(self.tc_min_n)
+        self.ws.tc_rand_slots = slots
+
     def autotune(self, sweeps: int = 3, candidates=(64, 256, 512, 1024, None),
                  seed: int = 1) -> dict:
         """Choose the tensor-core threshold (instances with n >= threshold
@@ -303,6 +332,8 @@ class PTBatch:
         recompute() once)."""
         if self.autotune_pending and update == "sequential" and num_sweeps:
             self.autotune()
+        if update == "random" and self.tc and num_sweeps:
+            self._setup_random_tc()
         if recompute_every is None:
             recompute_every = 4 if (self.tc and self.tc_terms == 2) else 0
         upd = _lib.RANDOM if update == "random" else _lib.SEQUENTIAL
@@ -337,8 +368,8 @@ class PTBatch:
             check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s),
                                           ref(self.ws), ref(opts), remaining,
                                           st), "sweeps")
-        if (final_recompute and recompute_every and upd == _lib.SEQUENTIAL
-                and self.tc):
+        if (final_recompute and recompute_every and self.tc and
+                (upd == _lib.SEQUENTIAL or self.ws.tc_rand_slots > 0)):
             self.recompute()
 
     def recompute(self):

@@ -167,3 +167,59 @@ def test_mixed_tc_and_plain_batch_bit_exact(oracle, kernel):
         assert (got["best_energy"][sl].reshape(Rd, R)
                 == want["best_energy"]).all()
         c0 += R * Rd
+
+
+@pytest.mark.parametrize("n,R", [(100, 4), (300, 3), (700, 4), (1300, 4),
+                                 (1300, 3)])
+def test_tc_random_order_bit_exact_vs_oracle(oracle, n, R):
+    """Random visiting order on the tensor cores (tiles repacked in each
+    sweep's shared permutation): same trajectories as the oracle's random
+    sweep, over more sweeps than the repacked-tile slots hold.  R = 4 divides
+    the chains per CTA (exchange inside the kernel); R = 3 does not (one
+    launch per sweep and a separate exchange)."""
+    rng = np.random.default_rng(2000 + n + R)
+    J, h = _int_qubo(rng, n)
+    Rd, sweeps = 3, 37
+    betas = (1.0 / np.geomspace(0.5, 8.0, R)).astype(np.float32)
+    x0 = rng.integers(0, 2, (Rd, R, n)).astype(np.float32)
+    e0 = np.array([[oracle.energy64(J, h, s) for s in r] for r in x0],
+                  np.float32)
+    got = _run("qubo", J, h, betas, x0, seed=n + R, sweeps=sweeps,
+               kernel="tc", update="random")
+    b = got["batch"]
+    assert b.ws.tc_rand_slots >= 1 and b.ws.tc_rand_slots < sweeps
+    want = oracle.pt_run("qubo", J, h, betas, x0, e0,
+                         np.tile(np.arange(R, dtype=np.int32), (Rd, 1)),
+                         seed=n + R, num_sweeps=sweeps, update="random")
+    assert (got["spins_f"] == want["spins"]).all()
+    assert (got["energies"].reshape(Rd, R) == want["energies"]).all()
+    assert (got["beta_idx"].reshape(Rd, R) == want["beta_idx"]).all()
+    assert (got["best_energy"].reshape(Rd, R) == want["best_energy"]).all()
+    assert (got["best_sweep"].reshape(Rd, R) == want["best_sweep"]).all()
+    assert (got["best_f"] == want["best_spins"]).all()
+
+
+def test_tc_random_order_mixed_batch_matches_plain():
+    """Random order in a batch whose small instance stays on the plain
+    kernel: both kernels follow the same permutations and streams."""
+    from pysa_gb300 import Instance, PTBatch, pack_spins
+    rng = np.random.default_rng(77)
+    sizes, R, Rd = [40, 260, 600], 4, 2
+    insts, x0s = [], []
+    for n in sizes:
+        J, h = _int_qubo(rng, n)
+        insts.append(Instance(J, h, (1.0 / np.geomspace(0.5, 8.0, R)
+                                     ).astype(np.float32), Rd))
+        x0s.append(rng.integers(0, 2, (Rd, R, n)).astype(np.float32))
+    out = {}
+    for kernel in ("auto", "plain"):
+        b = PTBatch("qubo", insts, kernel=kernel)
+        w = b.words
+        b.set_states(np.concatenate([pack_spins(x, "qubo", w).reshape(-1, w)
+                                     for x in x0s]), None)
+        b.run(21, seed=3, update="random")
+        out[kernel] = b.fetch()
+    assert b.tc is False
+    for k in ("spins", "energies", "beta_idx", "best_energy", "best_sweep",
+              "best_spins"):
+        assert (out["auto"][k] == out["plain"][k]).all(), k
