@@ -48,6 +48,8 @@ WORKLOADS = {
     "sk24_ais": dict(kind="ais", instances=64, n=24, temps=200, beta=2.0,
                      samples=1024, update="sequential"),
     # learned proposal vs plain PT, TTS(99%) (not an attempts/s line)
+    "rbm_mnist": dict(kind="rbm", visible=784, hidden=128, state_size=100,
+                      steps=1, tmin=1.0, tmax=1.0, parallel=False),
     "sk512_tts": dict(kind="pm1", n=512, replicas=64, reads=128, tmin=0.3,
                       tmax=3.0, instances=64, budgets=(1000, 4000, 16000),
                       target_sweeps=32000, update="sequential"),
@@ -535,6 +537,93 @@ def run_ais_workload(args, w, rank, world):
     return 0
 
 
+def run_rbm_workload(args, w, rank, world):
+    """RBM negative phase (tutorials/rbm_pysa.py:111-140 at the MNIST
+    tutorial's sizes): persistent-state updates per second through
+    RBM_PySA.update_states_with_pysa (problem, states and results on the
+    device), beside the reference's recipe on the same kernels (QUBO built
+    on the host, Solver, states copied back).  W moves a little before every
+    update, as an optimiser step would."""
+    if rank != 0:
+        return 0
+    import torch
+    from pysa_gb300 import Solver
+    from pysa_gb300.rbm import RBM_PySA
+    V, H, S = w["visible"], w["hidden"], w["state_size"]
+    n = V + H
+    torch.manual_seed(7)
+    m = RBM_PySA(V, H, state_size=S, steps=w["steps"], parallel=w["parallel"],
+                 min_temp=w["tmin"], max_temp=w["tmax"], seed=11)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    m.v_state = (torch.rand(S, V, device="cuda", generator=g) > 0.5).float()
+    m.h_state = (torch.rand(S, H, device="cuda", generator=g) > 0.5).float()
+
+    def nudge():
+        with torch.no_grad():
+            m.W.add_(1e-3 * torch.randn(V, H, device="cuda", generator=g))
+
+    def host_recipe(seed):
+        W = m.W.detach().cpu().numpy()
+        vb = m.v_bias.detach().cpu().numpy()
+        hb = m.h_bias.detach().cpu().numpy()
+        problem = np.zeros((n, n), np.float32)
+        problem[:V, V:] = W
+        problem[V:, :V] = W.T
+        problem += np.diag(np.concatenate([vb, hb]).squeeze())
+        x0 = torch.cat([m.v_state, m.h_state], 1).cpu().numpy()
+        res = Solver(-problem, "qubo", "float32").metropolis_update(
+            num_sweeps=w["steps"], num_reads=1, num_replicas=S,
+            update_strategy="sequential", min_temp=w["tmin"],
+            max_temp=w["tmax"], initialize_strategy=x0,
+            parallel=w["parallel"], seed=seed, return_dataframe=False)
+        st = torch.from_numpy(res[0]["states"]).cuda()
+        m.v_state, m.h_state = torch.split(st, V, dim=1)
+
+    for i in range(args.warmup):
+        nudge()
+        m.update_states_with_pysa(seed=i)
+    torch.cuda.synchronize()
+    K = max(1, min(args.steps, 500))
+    t0 = time.perf_counter()
+    for i in range(K):
+        nudge()
+        m.update_states_with_pysa(seed=1000 + i)
+    torch.cuda.synchronize()
+    dt_dev = (time.perf_counter() - t0) / K
+    m.negative_phase().item()
+    for i in range(args.warmup):
+        nudge()
+        host_recipe(i)
+    torch.cuda.synchronize()
+    Kh = max(1, min(K, 100))
+    t0 = time.perf_counter()
+    for i in range(Kh):
+        nudge()
+        host_recipe(2000 + i)
+    torch.cuda.synchronize()
+    dt_host = (time.perf_counter() - t0) / Kh
+    attempts = S * n * w["steps"]
+    print(json.dumps({
+        "metric": "rbm_negative_phase_updates_per_s", "value": 1.0 / dt_dev,
+        "unit": "updates/s", "n_gpus": 1, "steps": K,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt_dev,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded; W ~ N(0, 1) as the "
+        "reference initialises it)",
+        "config": {"workload": args.workload, **w, "n": n},
+        "attempts_per_s": attempts / dt_dev,
+        "host_round_trip": {
+            "ms_per_step": 1e3 * dt_host, "updates_per_s": 1.0 / dt_host,
+            "what": "reference recipe on the same kernels: QUBO assembled "
+                    "in NumPy, Solver.metropolis_update, states copied back"},
+        "e2e": {"value": 1.0 / dt_dev, "unit": "updates/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 1,
+                "note": "inputs and outputs are device tensors; one byte "
+                        "(the BF16-exactness flag of the new couplings) "
+                        "reaches the host per update"}}), flush=True)
+    return 0
+
+
 def _reference_sample(w):
     """(ptype, P, description) of the instance the reference arm times."""
     if w["kind"] == "sk_batch":
@@ -649,6 +738,16 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if w["kind"] == "rbm":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable":
+                                  "the reference's RBM caller runs "
+                                  "pysa.sa.Solver, which needs numba (absent "
+                                  "here); its host recipe is timed on the "
+                                  "GPU arm's line instead"}))
+            return 0
+        return run_rbm_workload(args, w, rank, world)
     if w["kind"] in ("sk_batch", "ais") and args.impl != "reference":
         fn = run_batch_workload if w["kind"] == "sk_batch" else run_ais_workload
         return fn(args, w, rank, world)

@@ -264,10 +264,35 @@ int pysa_gb_energy64(int32_t problem_type, int32_t n, int32_t ld64,
                      const uint32_t *spins, int32_t words, int64_t count,
                      double *out, void *stream);
 
+/* The same f64 energies with the couplings and fields of instance inst of
+ * the problem tables (f32, J stored transposed, values taken exactly). */
+int pysa_gb_energy64_tables(const pysa_gb_problems *p,
+                            const pysa_gb_host_tables *host, int32_t inst,
+                            const uint32_t *spins, int32_t words,
+                            int64_t count, double *out, void *stream);
+
 /* Unpack bit-packed spins into float32 values (+-1 or 0/1), [count, n]. */
 int pysa_gb_unpack(int32_t problem_type, int32_t n, const uint32_t *spins,
                    int32_t words, int64_t count, float *out, int32_t out_ld,
                    void *stream);
+
+/* Pack float32 states on the device ([count, x_ld], +-1 or 0/1; the bit is
+ * x > 0 for Ising, x != 0 for QUBO) into bit-packed words [count, words]:
+ * the device-side form of the initial states handed to
+ * simulation_parallel (pysa/sa.py:303-313). */
+int pysa_gb_pack(int32_t problem_type, int32_t n, const float *x,
+                 int32_t x_ld, int64_t count, uint32_t *spins, int32_t words,
+                 void *stream);
+
+/* Replace instance inst's couplings and local fields (writes p->J and p->h,
+ * which must be writable device memory) from a dense symmetric problem
+ * matrix P in device memory (n x n, row stride p_ld), split as
+ * Solver.__init__ does (pysa/sa.py:66-69): couplings = P with a zero
+ * diagonal, fields = diag(P).  The caller then re-runs pysa_gb_setup (and
+ * pysa_gb_tc_setup) so the sweep kernels' copies of J follow. */
+int pysa_gb_load_problem(const pysa_gb_problems *p,
+                         const pysa_gb_host_tables *host, int32_t inst,
+                         const float *P, int32_t p_ld, void *stream);
 
 /* Annealed importance sampling (Solver.annealed_importance, pysa/sa.py:432-553;
  * ais_sample, pysa/simulation.py:293-317; update_spin_ref,

@@ -113,6 +113,10 @@ def load() -> ctypes.CDLL:
         "pysa_gb_energy64": ([I32, I32, I32, P, P, P, I32, I64, P, P],
                              ctypes.c_int),
         "pysa_gb_unpack": ([I32, I32, P, I32, I64, P, I32, P], ctypes.c_int),
+        "pysa_gb_pack": ([I32, I32, P, I32, I64, P, I32, P], ctypes.c_int),
+        "pysa_gb_energy64_tables": ([P, P, I32, P, I32, I64, P, P],
+                                    ctypes.c_int),
+        "pysa_gb_load_problem": ([P, P, I32, P, I32, P], ctypes.c_int),
         "pysa_gb_ais": ([P, P, P, P, P, P, P], ctypes.c_int),
         "pysa_gb_logz_parts": ([I32, I32], I64),
         "pysa_gb_logz_exact": ([P, ctypes.c_double, P, P, P], ctypes.c_int),

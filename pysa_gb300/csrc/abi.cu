@@ -605,6 +605,49 @@ int pysa_gb_unpack(int32_t problem_type, int32_t n, const uint32_t* spins,
   return PYSA_GB_OK;
 }
 
+int pysa_gb_energy64_tables(const pysa_gb_problems* p,
+                            const pysa_gb_host_tables* host, int32_t inst,
+                            const uint32_t* spins, int32_t words,
+                            int64_t count, double* out, void* stream) {
+  if (!p || !host || !spins || !out || inst < 0 ||
+      inst >= p->num_instances || count < 0)
+    return fail(PYSA_GB_ERR_ARG, "energy64_tables: bad argument");
+  if (words < (host->n[inst] + 31) / 32)
+    return fail(PYSA_GB_ERR_ARG, "energy64_tables: words too small");
+  launch_energy64_tables(*p, inst, spins, words, count, out,
+                         (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "energy64_tables");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_pack(int32_t problem_type, int32_t n, const float* x,
+                 int32_t x_ld, int64_t count, uint32_t* spins, int32_t words,
+                 void* stream) {
+  if (!x || !spins || n < 1 || x_ld < n || count < 0 ||
+      words < (n + 31) / 32)
+    return fail(PYSA_GB_ERR_ARG, "pack: bad argument");
+  launch_pack(problem_type, n, x, x_ld, count, spins, words,
+              (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "pack");
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_load_problem(const pysa_gb_problems* p,
+                         const pysa_gb_host_tables* host, int32_t inst,
+                         const float* P, int32_t p_ld, void* stream) {
+  if (!p || !host || !P || inst < 0 || inst >= p->num_instances)
+    return fail(PYSA_GB_ERR_ARG, "load_problem: bad argument");
+  const int n = host->n[inst], ld = host->ld[inst];
+  if (n < 1 || p_ld < n || ld < n)
+    return fail(PYSA_GB_ERR_ARG, "load_problem: bad sizes");
+  launch_load_problem(*p, inst, n, ld, P, p_ld, (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "load_problem");
+  return PYSA_GB_OK;
+}
+
 int pysa_gb_ais(const pysa_gb_problems* p, pysa_gb_state* s,
                 pysa_gb_workspace* ws, const pysa_gb_ais_options* o,
                 const float* temps, double* log_w, void* stream) {

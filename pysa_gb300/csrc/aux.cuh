@@ -43,7 +43,14 @@ void launch_perm(const PermArgs& a, cudaStream_t st, int count = 1);
 void launch_energy64(int ptype, int n, int ld, const double* J,
                      const double* h, const uint32_t* spins, int words,
                      int64_t count, double* out, cudaStream_t st);
+void launch_energy64_tables(const pysa_gb_problems& p, int inst,
+                            const uint32_t* spins, int words, int64_t count,
+                            double* out, cudaStream_t st);
 void launch_unpack(int ptype, int n, const uint32_t* spins, int words,
                    int64_t count, float* out, int out_ld, cudaStream_t st);
+void launch_pack(int ptype, int n, const float* x, int x_ld, int64_t count,
+                 uint32_t* spins, int words, cudaStream_t st);
+void launch_load_problem(const pysa_gb_problems& p, int inst, int n, int ld,
+                         const float* P, int p_ld, cudaStream_t st);
 
 }  // namespace pysa_gb

@@ -30,14 +30,17 @@ void launch_pack_rows(const float* J, int ld, int n, int nc, int ls,
 }
 
 // -------------------------------------------------- fields and energies
-// Warp per chain.  F_i = sum_j J_ij s_j in f64, from f32 partial sums over 32
-// rows (the products J_ij s_j are exact in f32); H_i = f32(F_i + h_i);
-// E = sum_i s_i (F_i / 2 + h_i)  (pysa/ising.py:37, pysa/qubo.py:37).
-__global__ void k_fields(const PrepArgs a) {
-  const int warps = blockDim.x >> 5;
-  const int64_t c = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (c >= a.p.num_chains) return;
+// CTA per chain, warp per chunk of 256 columns (8 per lane).  F_i = sum_j
+// J_ij s_j in f64, from f32 partial sums over 32 rows (the products J_ij s_j
+// are exact in f32); H_i = f32(F_i + h_i); E = sum_i s_i (F_i / 2 + h_i)
+// (pysa/ising.py:37, pysa/qubo.py:37), summed per lane, then over the warp,
+// then over the chunks in order, so the result does not depend on timing.
+constexpr int kFieldWarps = 8;
+__global__ void __launch_bounds__(32 * kFieldWarps) k_fields(const PrepArgs a) {
+  __shared__ double e_s[kFieldWarps];
+  const int64_t c = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
   // instance of chain c: binary search over chain_off
   int lo = 0, hi = a.p.num_instances - 1;
   while (lo < hi) {
@@ -51,8 +54,8 @@ __global__ void k_fields(const PrepArgs a) {
   const float* h = a.p.h + a.p.h_off[inst];
   const uint32_t* sw = a.s.spins + c * a.p.words;
   double e = 0.0;
-  constexpr int TC = 8;  // columns per lane per pass
-  for (int base = 0; base < n; base += 32 * TC) {
+  constexpr int TC = 8;  // columns per lane per chunk
+  for (int base = 256 * warp; base < n; base += 256 * nwarps) {
     double F[TC];
     float part[TC];
 #pragma unroll
@@ -79,33 +82,38 @@ __global__ void k_fields(const PrepArgs a) {
         }
       }
     }
+    double ec = 0.0;
 #pragma unroll
     for (int k = 0; k < TC; ++k) {
       const int col = base + 32 * k + lane;
       if (col < n) {
         const uint32_t bit = (sw[col >> 5] >> (col & 31)) & 1u;
         const double si = bit ? 1.0 : (ising ? -1.0 : 0.0);
-        e += si * (0.5 * F[k] + (double)h[col]);
+        ec += si * (0.5 * F[k] + (double)h[col]);
         a.fields[c * a.field_ld + col] = (float)(F[k] + (double)h[col]);
       }
     }
+    e += warp_sum(ec);
   }
-  e = warp_sum(e);
-  if (lane == 0 && a.set_energies) a.s.energies[c] = (float)e;
+  if (lane == 0) e_s[warp] = e;
+  __syncthreads();
+  if (threadIdx.x == 0 && a.set_energies) {
+    double t = 0.0;
+    for (int w = 0; w < nwarps; ++w) t += e_s[w];
+    a.s.energies[c] = (float)t;
+  }
 }
 
-// chain_beta from beta_idx (pysa/simulation.py:151-152) and best init.
+// CTA per read, thread per replica: the slot betas and the initial best.
 __global__ void k_read_init(const PrepArgs a) {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= a.p.num_reads) return;
+  const int64_t r = blockIdx.x;
   const int inst = a.p.read_inst[r];
   const int R = a.p.replicas[inst];
   const int64_t base = a.p.chain_off[inst] + (r - a.p.read_off[inst]) * R;
   const float* betas = a.p.ladder + a.p.ladder_off[inst];
-  for (int k = 0; k < R; ++k)
+  for (int k = threadIdx.x; k < R; k += blockDim.x) {
     a.s.chain_beta[base + a.s.beta_idx[base + k]] = betas[k];
-  if (a.init_best) {
-    for (int k = 0; k < R; ++k) {
+    if (a.init_best) {
       const int64_t c = base + k;
       a.s.best_energy[c] = a.best_global ? __int_as_float(0x7f800000)
                                          : a.s.energies[c];
@@ -118,12 +126,12 @@ __global__ void k_read_init(const PrepArgs a) {
 
 void launch_prepare(const PrepArgs& a, cudaStream_t st) {
   if (a.p.num_chains > 0) {
-    const int warps = 4;
-    const int64_t blocks = (a.p.num_chains + warps - 1) / warps;
-    k_fields<<<(unsigned)blocks, warps * 32, 0, st>>>(a);
+    int warps = (a.p.max_n + 255) / 256;
+    warps = warps < 1 ? 1 : warps > kFieldWarps ? kFieldWarps : warps;
+    k_fields<<<(unsigned)a.p.num_chains, warps * 32, 0, st>>>(a);
   }
   if (a.p.num_reads > 0)
-    k_read_init<<<(unsigned)((a.p.num_reads + 127) / 128), 128, 0, st>>>(a);
+    k_read_init<<<(unsigned)a.p.num_reads, 128, 0, st>>>(a);
 }
 
 // ------------------------------------------------------ replica exchange
@@ -244,42 +252,71 @@ void launch_perm(const PermArgs& a, cudaStream_t st, int count) {
 }
 
 // ----------------------------------------------------------- f64 energy
-// Warp per state: E = sum_i s_i (sum_j J_ij s_j / 2 + h_i) in f64.
-__global__ void k_energy64(int ptype, int n, int ld, const double* J,
-                           const double* h, const uint32_t* spins, int words,
-                           int64_t count, double* out) {
-  const int warps = blockDim.x >> 5;
-  const int64_t c = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (c >= count) return;
+// CTA per state, warp per row i (rows warp, warp + 8, ...), lanes over the
+// columns: f_i = sum_j J_ij s_j, E = sum_i s_i (f_i / 2 + h_i) in f64,
+// reduced in a fixed order (lanes, then rows of a warp, then warps).
+template <typename T>
+__device__ __forceinline__ void energy64_body(
+    int ptype, int n, int ld, const T* J, const T* h, const uint32_t* spins,
+    int words, double* out) {
+  __shared__ double e_s[8];
+  const int64_t c = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t* sw = spins + c * words;
   const bool ising = ptype == PYSA_GB_ISING;
   double e = 0.0;
-  for (int i = lane; i < n; i += 32) {
-    const double si = ((sw[i >> 5] >> (i & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
-    if (si == 0.0) continue;
+  for (int i = warp; i < n; i += 8) {
+    const double si =
+        ((sw[i >> 5] >> (i & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+    if (si == 0.0) continue;  // warp-uniform
+    const T* row = J + (int64_t)i * ld;
     double f = 0.0;
-    const double* row = J + (int64_t)i * ld;
-    for (int j = 0; j < n; ++j) {
+    for (int j = lane; j < n; j += 32) {
       const double sj =
           ((sw[j >> 5] >> (j & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
-      f += row[j] * sj;
+      f += (double)row[j] * sj;
     }
-    e += si * (0.5 * f + h[i]);
+    f = warp_sum(f);
+    e += si * (0.5 * f + (double)h[i]);
   }
-  e = warp_sum(e);
-  if (lane == 0) out[c] = e;
+  if (lane == 0) e_s[warp] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += e_s[w];
+    out[c] = t;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_energy64(
+    int ptype, int n, int ld, const double* J, const double* h,
+    const uint32_t* spins, int words, double* out) {
+  energy64_body<double>(ptype, n, ld, J, h, spins, words, out);
+}
+
+// Same with instance inst's f32 couplings and fields of the problem tables.
+__global__ void __launch_bounds__(256) k_energy64_tables(
+    const pysa_gb_problems p, int inst, const uint32_t* spins, int words,
+    double* out) {
+  energy64_body<float>(p.problem_type, p.n[inst], p.ld[inst],
+                       p.J + p.j_off[inst], p.h + p.h_off[inst], spins, words,
+                       out);
 }
 
 void launch_energy64(int ptype, int n, int ld, const double* J,
                      const double* h, const uint32_t* spins, int words,
                      int64_t count, double* out, cudaStream_t st) {
-  const int warps = 4;
-  const int64_t blocks = (count + warps - 1) / warps;
-  if (blocks > 0)
-    k_energy64<<<(unsigned)blocks, warps * 32, 0, st>>>(ptype, n, ld, J, h,
-                                                        spins, words, count,
-                                                        out);
+  if (count > 0)
+    k_energy64<<<(unsigned)count, 256, 0, st>>>(ptype, n, ld, J, h, spins,
+                                                words, out);
+}
+
+void launch_energy64_tables(const pysa_gb_problems& p, int inst,
+                            const uint32_t* spins, int words, int64_t count,
+                            double* out, cudaStream_t st) {
+  if (count > 0)
+    k_energy64_tables<<<(unsigned)count, 256, 0, st>>>(p, inst, spins, words,
+                                                       out);
 }
 
 // ---------------------------------------------------------------- unpack
@@ -303,6 +340,70 @@ void launch_unpack(int ptype, int n, const uint32_t* spins, int words,
   if (blocks > 0)
     k_unpack<<<(unsigned)blocks, 256, 0, st>>>(ptype, n, spins, words, count,
                                                out, out_ld);
+}
+
+// Float states (+-1 or 0/1) -> bit-packed words: a warp per (state, word),
+// one ballot per word.  The bit is x > 0 (Ising) or x != 0 (QUBO), the rule
+// of the host-side packing.
+__global__ void k_pack(int ptype, int n, const float* x, int x_ld,
+                       int64_t count, uint32_t* spins, int words) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = count * words;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+       e < total; e += nw) {
+    const int64_t c = e / words;
+    const int w = (int)(e % words);
+    const int j = 32 * w + lane;
+    bool b = false;
+    if (j < n) {
+      const float v = x[c * x_ld + j];
+      b = ptype == PYSA_GB_ISING ? v > 0.0f : v != 0.0f;
+    }
+    const uint32_t bits = __ballot_sync(0xffffffffu, b);
+    if (lane == 0) spins[c * words + w] = bits;
+  }
+}
+
+void launch_pack(int ptype, int n, const float* x, int x_ld, int64_t count,
+                 uint32_t* spins, int words, cudaStream_t st) {
+  const int64_t warps = count * words;
+  int64_t blocks = (warps + 7) / 8;
+  if (blocks > 65535) blocks = 65535;
+  if (blocks > 0)
+    k_pack<<<(unsigned)blocks, 256, 0, st>>>(ptype, n, x, x_ld, count, spins,
+                                             words);
+}
+
+// A dense symmetric problem matrix P (n x n, row stride p_ld) of instance
+// inst split as the reference's Solver does (pysa/sa.py:66-69): couplings =
+// P with a zero diagonal, stored transposed (row j = column j of P), and
+// local fields = diag(P).
+__global__ void k_load_problem(const pysa_gb_problems p, int inst,
+                               const float* P, int p_ld) {
+  const int n = p.n[inst];
+  const int ld = p.ld[inst];
+  // the tables' J and h are const for the sweeps; this kernel refills them
+  float* Jt = const_cast<float*>(p.J) + p.j_off[inst];
+  float* h = const_cast<float*>(p.h) + p.h_off[inst];
+  const int64_t total = (int64_t)n * ld;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e / ld), i = (int)(e % ld);
+    float v = 0.0f;
+    if (i < n && i != j) v = P[(int64_t)i * p_ld + j];
+    Jt[e] = v;
+    if (i == j) h[j] = P[(int64_t)j * p_ld + j];
+  }
+}
+
+void launch_load_problem(const pysa_gb_problems& p, int inst, int n, int ld,
+                         const float* P, int p_ld, cudaStream_t st) {
+  const int64_t total = (int64_t)n * ld;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 65535) blocks = 65535;
+  if (blocks > 0)
+    k_load_problem<<<(unsigned)blocks, 256, 0, st>>>(p, inst, P, p_ld);
 }
 
 }  // namespace pysa_gb

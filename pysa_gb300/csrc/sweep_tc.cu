@@ -529,12 +529,43 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             }
             uint32_t w0 = o0, w1 = o1;
             float dEb = 0.0f;
+            // Decisions in field units: with x = +-h signed so that
+            // dn = scale * x, a flip is certain when x >= th and excluded
+            // when x < tl.  th and tl bracket log(u) / (beta * scale) by the
+            // f32 band of log(u), 3e-5 + 1e-6 |log u| (over three times the
+            // error of __logf plus the two roundings of a threshold); in
+            // between, the exact f64 rule decides.  With beta <= 0 every
+            // flip is accepted (log u < 0 <= beta * dn).
+            const float scale = ising ? 2.0f : 1.0f;
+            const bool bpos = beta > 0.0f;
+            const float invbs = bpos ? 1.0f / (beta * scale) : 0.0f;
+            // the previous sub-block's deltas (its corrections of this one
+            // and its A rows come from registers)
+            float dprev[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) dprev[j] = 0.0f;
             bool a_ok = true;
-            // four sub-blocks of 16 spins; corrections from earlier sub-blocks
-            // are applied lazily when a sub-block's fields are loaded
-    #pragma unroll 1
-            for (int g = 0; g < 4; ++g) {
-              float hs[16];
+            // one sub-block's deltas into the A rows of every slice
+            auto put_a = [&](int gg, const float* d) {
+              uint32_t pkg[8];
+#pragma unroll
+              for (int j = 0; j < 16; j += 2)
+                pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
+#pragma unroll
+              for (int qq = 0; qq < F; ++qq) {
+                const int m = qq * CC + c;
+                unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                      ((m >> 3) * 8) * 128 + (m & 7) * 16;
+                *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
+                    make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+                *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
+                    make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
+              }
+            };
+            // fields of sub-block g with the corrections of every earlier
+            // sub-block of the block (again = a redo: the fields are read
+            // once more)
+            auto fields = [&](int g, bool again, float* hs) {
               if constexpr (!RND) {
                 tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
               } else if constexpr (F > 1) {
@@ -552,64 +583,90 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                     r[j] = tc::tmem_ld1_nowait(taddr + lane_base +
                                                (uint32_t)sp);
                 }
-                tc::tmem_wait_ld();
+                tc::tmem_wait_ld16(r);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) hs[j] = __uint_as_float(r[j]);
               }
-              if (lead) stamp(a, Gb, 8 + 3 * g);
-              // with helpers, sub-blocks older than g-1 arrive precomputed
-              const int k_lo = (C::HELP && g >= 2) ? 16 * (g - 1) : 0;
+              if (lead && !again) stamp(a, Gb, 8 + 3 * g);
+              // sub-blocks before the previous one: precomputed by the
+              // helpers (fold 2) or from the deltas in shared memory
               if (C::HELP && g >= 2) {
     #pragma unroll
                 for (int j = 0; j < 16; ++j)
                   hs[j] += corr_s[((g - 2) * 16 + j) * CC + c];
-              }
+              } else {
     #pragma unroll 2
-              for (int k = k_lo; k < 16 * g; ++k) {
-                const float d = dl_s[k * CC + c];
-                const float4* jr =
-                    reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
+                for (int k = 0; k < 16 * (g - 1); ++k) {
+                  const float d = dl_s[k * CC + c];
+                  const float4* jr =
+                      reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
     #pragma unroll
-                for (int q4 = 0; q4 < 4; ++q4) {
-                  const float4 v = jr[q4];
-                  hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
-                  hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
-                  hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
-                  hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
+                  for (int q4 = 0; q4 < 4; ++q4) {
+                    const float4 v = jr[q4];
+                    hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
+                    hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
+                    hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
+                    hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
+                  }
                 }
               }
+              // the previous sub-block, from registers
+              if (g > 0) {
+    #pragma unroll
+                for (int kk = 0; kk < 16; ++kk) {
+                  const float d = dprev[kk];
+                  const float4* jr = reinterpret_cast<const float4*>(
+                      jb + (16 * (g - 1) + kk) * 64 + 16 * g);
+    #pragma unroll
+                  for (int q4 = 0; q4 < 4; ++q4) {
+                    const float4 v = jr[q4];
+                    hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
+                    hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
+                    hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
+                    hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
+                  }
+                }
+              }
+            };
+            // four sub-blocks of 16 spins
+    #pragma unroll 1
+            for (int g = 0; g < 4; ++g) {
+              float hs[16];
+              fields(g, false, hs);
               if (lead) stamp(a, Gb, 9 + 3 * g);
               uint32_t wcur = g < 2 ? w0 : w1;
               const int sb = 16 * (g & 1);
+              const uint32_t sbits = wcur >> sb;  // spins before the sub-block
+              float lfv[16];
+#pragma unroll
+              for (int j = 0; j < 16; ++j) lfv[j] = lfb[(16 * g + j) * CC + c];
 
-              // fast pass: branch-free decisions from the precomputed log-uniform;
-              // a decision inside the f32 error band is only flagged here
+              // fast pass: branch-free decisions on the thresholds; a
+              // decision inside the band is only flagged here.  No shared
+              // memory stores inside, so the loads of later rows are free to
+              // move ahead of earlier decisions
               const uint32_t wsave = wcur;
               const float dEsave = dEb;
-              float hsave[16];
-    #pragma unroll
-              for (int j = 0; j < 16; ++j) hsave[j] = hs[j];
               bool unc = false;
+              float dcur[16];
     #pragma unroll
               for (int j = 0; j < 16; ++j) {
                 const int k = 16 * g + j;
-                const bool sbit = (wcur >> (sb + j)) & 1u;
-                const float hk = hs[j];
-                const float dn =
-                    ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
-                const float lfk = lfb[k * CC + c];
-                const float bd = beta * dn;
-                const float margin = 3e-5f + 1e-6f * fabsf(bd);
+                const float lfk = lfv[j];
+                const float m = fmaf(1e-6f, fabsf(lfk), 3e-5f);
                 const bool live = valid && k < kmax;
-                const bool yes = dn >= 0.0f || lfk < bd - margin;
-                const bool no = bd < -24.0f || lfk > bd + margin;
-                unc |= live && !yes && !no;
-                const bool acc = live && yes;
-                const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
-                                              : (sbit ? -1.0f : 1.0f))
-                                     : 0.0f;
-                dl_s[k * CC + c] = dl;
-                dEb = acc ? dEb - dn : dEb;
+                const float th =
+                    !live ? INFINITY
+                          : bpos ? fminf((lfk + m) * invbs, 0.0f) : -INFINITY;
+                const float tl =
+                    !live ? INFINITY : bpos ? (lfk - m) * invbs : -INFINITY;
+                const bool sbit = (sbits >> j) & 1u;
+                const float x = sbit ? hs[j] : -hs[j];
+                const bool acc = x >= th;
+                unc |= !acc && !(x < tl);
+                const float dl = acc ? (sbit ? -scale : scale) : 0.0f;
+                dcur[j] = dl;
+                dEb = acc ? fmaf(-scale, x, dEb) : dEb;
                 wcur ^= acc ? (1u << (sb + j)) : 0u;
                 if (j < 15) {  // exact corrections inside the sub-block
                   const float4* jr =
@@ -625,11 +682,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 }
               }
               if (__any_sync(0xffffffffu, unc)) {
-                // rare: redo the sub-block with the exact f64 rule where needed
+                // rare: redo the sub-block with the exact f64 rule where
+                // needed, from freshly rebuilt fields
                 wcur = wsave;
                 dEb = dEsave;
-    #pragma unroll
-                for (int j = 0; j < 16; ++j) hs[j] = hsave[j];
+                fields(g, true, hs);
     #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                   const int k = 16 * g + j;
@@ -639,13 +696,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                       ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
                   const bool acc =
                       valid && k < kmax &&
-                      metropolis_accept_lf(dn, beta, lfb[k * CC + c], a.seed,
+                      metropolis_accept_lf(dn, beta, lfv[j], a.seed,
                                            (uint32_t)inst, sweep, chain_local,
                                            (uint32_t)(i0 + k));
                   const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
                                                 : (sbit ? -1.0f : 1.0f))
                                        : 0.0f;
-                  dl_s[k * CC + c] = dl;
+                  dcur[j] = dl;
                   if (acc) {
                     dEb -= dn;
                     wcur ^= 1u << (sb + j);
@@ -665,36 +722,24 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 }
               }
               if (g < 2) w0 = wcur; else w1 = wcur;
+#pragma unroll
+              for (int j = 0; j < 16; ++j) dl_s[(16 * g + j) * CC + c] = dcur[j];
+              // deltas into the A rows.  A is single-buffered: the previous
+              // block's MMAs must be done first; waiting after the second
+              // sub-block leaves them that long to finish
+              if (g == 1 && Gb > G0) {
+                if (lead) stamp(a, Gb, 2);
+                a_ok = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
+                if (lead) stamp(a, Gb, 3);
+              }
+              if (a_ok && g >= 1) {
+                if (g == 1) put_a(0, dprev);
+                put_a(g, dcur);
+              }
+#pragma unroll
+              for (int j = 0; j < 16; ++j) dprev[j] = dcur[j];
               if (lead) stamp(a, Gb, 10 + 3 * g);
               if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
-            }
-            // the block's deltas (kept in dl_s) into the A rows; A is
-            // single-buffered, so the previous block's MMAs must be done (they
-            // normally finished while this block was being decided)
-            if (Gb > G0) {
-              if (lead) stamp(a, Gb, 2);
-              a_ok = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
-              if (lead) stamp(a, Gb, 3);
-            }
-            if (a_ok) {
-    #pragma unroll 1
-              for (int g = 0; g < 4; ++g) {
-                uint32_t pkg[8];
-    #pragma unroll
-                for (int j = 0; j < 16; j += 2)
-                  pkg[j >> 1] = bf16_bits(dl_s[(16 * g + j) * CC + c]) |
-                                (bf16_bits(dl_s[(16 * g + j + 1) * CC + c]) << 16);
-    #pragma unroll
-                for (int qq = 0; qq < F; ++qq) {
-                  const int m = qq * CC + c;
-                  unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                        ((m >> 3) * 8) * 128 + (m & 7) * 16;
-                  *reinterpret_cast<uint4*>(rowp + (2 * g) * 128) =
-                      make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
-                  *reinterpret_cast<uint4*>(rowp + (2 * g + 1) * 128) =
-                      make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
-                }
-              }
             }
             if (valid) {
               if constexpr (!RND) {

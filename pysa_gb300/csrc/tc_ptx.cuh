@@ -80,6 +80,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Waits for this thread's TMEM loads; the 16 registers of the last one are
+// operands of the wait, so no use of them is scheduled above it.
+__device__ __forceinline__ void tmem_wait_ld16(uint32_t* r) {
+  __syncwarp();
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]),
+                 "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]),
+                 "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+                 "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+
 // One column (32 lanes x 1) without waiting: the register is valid only
 // after tmem_wait_ld(); a warp gathers scattered columns with one wait.
 __device__ __forceinline__ uint32_t tmem_ld1_nowait(uint32_t taddr) {

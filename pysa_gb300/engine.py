@@ -63,18 +63,23 @@ class PTBatch:
 
     def __init__(self, problem_type: str, instances: list[Instance],
                  device: torch.device | str | None = None,
-                 perm_slots: int = 1, kernel: str = "auto"):
+                 perm_slots: int = 1, kernel: str = "auto",
+                 tc_terms: int | None = None):
         """kernel: 'plain' (CUDA-core sweep for every instance), 'tc'
         (tensor-core blocked sweep for every instance, sequential order,
         64 <= n <= 2048), 'auto' (tensor cores for the instances with
         64 <= n <= 2048, the plain kernel for the rest, in the same sweep)
         or 'autotune' ('auto' until autotune() picks the threshold by
-        timing; run() calls it on first use)."""
+        timing; run() calls it on first use).  tc_terms sizes the
+        tensor-core tiles for 1 or 2 BF16 terms (default: 1 when every J is
+        exactly BF16); load_problem() needs room for 2 when later couplings
+        may not be."""
         if not torch.cuda.is_available():
             raise RuntimeError(
                 "pysa_gb300 needs a CUDA GPU: the sweeps run only as "
                 "sm_103a kernels (no CPU path)")
         self.lib = _lib.load()
+        self._tc_terms_req = tc_terms
         self.device = torch.device(device or "cuda")
         self.problem_type = problem_type
         self.ptype = _lib.ISING if problem_type == "ising" else _lib.QUBO
@@ -202,6 +207,8 @@ class PTBatch:
         if not hasattr(self, "tc_b"):
             # sized once for the widest selection (every instance >= 64)
             terms = 1 if all(bf16_exact(x.J) for x in self.instances) else 2
+            if self._tc_terms_req is not None:
+                terms = max(terms, int(self._tc_terms_req))
             tneed = (ctypes.c_int64 * 3)()
             titems = check(self.lib.pysa_gb_tc_workspace(
                 I, ref(ht_), terms, 64, tneed), "tc sizing")
@@ -221,6 +228,7 @@ class PTBatch:
             self.ws.tc_sched = _ptr(self.tc_sched)
             self.ws.tc_terms = terms
             self.tc_terms = terms
+            self._tc_terms_cap = terms
         self.ws.tc_min_n = int(min_n)
         check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(ht_), ref(self.ws),
                                         self._stream.cuda_stream), "tc setup")
@@ -293,6 +301,83 @@ class PTBatch:
         self.autotune_pending = False
         self.autotune_ms = times
         return times
+
+    # ---------------------------------------------- device-resident inputs
+    def load_problem(self, inst: int, P: torch.Tensor):
+        """Couplings and fields of instance `inst` from a dense symmetric
+        problem matrix in device memory, split on the device as
+        pysa/sa.py:66-69 does; the kernels' packed copies of J are rebuilt
+        on the device.  Only the BF16-exactness flag of P (one byte) comes
+        to the host."""
+        n = int(self.n[inst])
+        P = P.detach().to(device=self.device, dtype=torch.float32)
+        if P.shape != (n, n):
+            raise ValueError(f"problem must be {n} x {n}")
+        P = P.contiguous()
+        st = self._stream.cuda_stream
+        check(self.lib.pysa_gb_load_problem(ref(self.p), ref(self._ht),
+                                            int(inst), _ptr(P), n, st),
+              "load_problem")
+        check(self.lib.pysa_gb_setup(ref(self.p), ref(self._ht),
+                                     ref(self.ws), st), "setup")
+        if self.tc:
+            exact = bool((P.to(torch.bfloat16).to(torch.float32) == P).all())
+            terms = 1 if exact else 2
+            if terms > self._tc_terms_cap:
+                raise ValueError("couplings are not exact in BF16: build "
+                                 "the batch with tc_terms=2")
+            self.ws.tc_terms = terms
+            self.tc_terms = terms
+            check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(self._ht),
+                                            ref(self.ws), st), "tc setup")
+        self._graphs = {}
+        self._P_keep = P  # alive until the stream has read it
+
+    def set_states_device(self, states: torch.Tensor, energies=None,
+                          best_global: bool = False):
+        """Chains from device float states [num_chains, n] (+-1 or 0/1) of a
+        batch whose instances share n, packed on the device; energies
+        [num_chains] (device or host) or None to compute them with the
+        fields.  Temperature slots restart at 0..R-1 (pysa/sa.py:325)."""
+        n = int(self.n[0]) if len(self.n) else 0
+        if len(self.n) and (self.n != n).any():
+            raise ValueError("set_states_device needs one n for the batch")
+        x = states.detach().to(device=self.device, dtype=torch.float32)
+        x = x.reshape(self.num_chains, n).contiguous()
+        st = self._stream.cuda_stream
+        check(self.lib.pysa_gb_pack(self.ptype, n, _ptr(x), n,
+                                    self.num_chains, _ptr(self.spins),
+                                    self.words, st), "pack")
+        if energies is not None:
+            self.energies.copy_(torch.as_tensor(energies).reshape(-1).to(
+                device=self.device, dtype=torch.float32))
+        if not hasattr(self, "_bidx0"):
+            self._bidx0 = torch.from_numpy(np.concatenate([
+                np.tile(np.arange(self.R[i], dtype=np.int32), self.Rd[i])
+                for i in range(len(self.instances))
+            ]) if self.num_chains else np.zeros(1, np.int32)).to(self.device)
+        self.beta_idx.copy_(self._bidx0)
+        self.sweep_counter.zero_()
+        self.status.zero_()
+        self.ticket.zero_()
+        self.best_global = bool(best_global)
+        self._x_keep = x
+        check(self.lib.pysa_gb_prepare(ref(self.p), ref(self.s), ref(self.ws),
+                                       int(energies is None), 1,
+                                       int(best_global), st), "prepare")
+
+    def unpack_device(self, spins_words: torch.Tensor | None = None,
+                      dtype=torch.float32) -> torch.Tensor:
+        """Bit-packed device chains (default: the current ones) as device
+        floats [rows, n] (+-1 or 0/1), unpacked on the device."""
+        w = self.spins if spins_words is None else spins_words
+        n = int(self.n[0])
+        out = torch.empty(w.shape[0], n, dtype=torch.float32,
+                          device=self.device)
+        check(self.lib.pysa_gb_unpack(self.ptype, n, _ptr(w), self.words,
+                                      w.shape[0], _ptr(out), n,
+                                      self._stream.cuda_stream), "unpack")
+        return out if dtype == torch.float32 else out.to(dtype)
 
     # ------------------------------------------------------------ states
     def set_states(self, spins_words: np.ndarray, energies=None,

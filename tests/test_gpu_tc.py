@@ -76,6 +76,34 @@ def test_tc_matches_plain_kernel_ising_pm1():
         assert (a[k] == b[k]).all(), k
 
 
+@pytest.mark.parametrize("ptype,n", [("qubo", 256), ("ising", 320),
+                                     ("qubo", 1500)])
+def test_tc_extreme_betas_bit_exact_vs_oracle(oracle, ptype, n):
+    """beta = 0 (every flip accepted), tiny and very large betas: the
+    threshold form of the decision must agree with the f64 rule there."""
+    rng = np.random.default_rng(77 + n)
+    if ptype == "qubo":
+        J, h = _int_qubo(rng, n)
+        x0 = rng.integers(0, 2, (3, 6, n)).astype(np.float32)
+    else:
+        P = np.triu(2 * rng.integers(0, 2, (n, n)) - 1, 1)
+        J = (P + P.T).astype(np.float32)
+        h = rng.integers(-2, 3, n).astype(np.float32)
+        x0 = (2 * rng.integers(0, 2, (3, 6, n)) - 1).astype(np.float32)
+    betas = np.array([0.0, 1e-3, 0.05, 1.0, 8.0, 40.0], np.float32)
+    Rd, R = x0.shape[:2]
+    e0 = np.array([[oracle.energy64(J, h, s) for s in r] for r in x0],
+                  np.float32)
+    got = _run(ptype, J, h, betas, x0, seed=9, sweeps=5, kernel="tc")
+    want = oracle.pt_run(ptype, J, h, betas, x0, e0,
+                         np.tile(np.arange(R, dtype=np.int32), (Rd, 1)),
+                         seed=9, num_sweeps=5)
+    assert (got["spins_f"] == want["spins"]).all()
+    assert (got["energies"].reshape(Rd, R) == want["energies"]).all()
+    assert (got["beta_idx"].reshape(Rd, R) == want["beta_idx"]).all()
+    assert (got["best_energy"].reshape(Rd, R) == want["best_energy"]).all()
+
+
 @pytest.mark.parametrize("n", [320, 1024])
 def test_tc_split_bf16_energy_error(oracle, n):
     """Real couplings: J = J_hi + J_lo; energies within 1e-5 relative of an
