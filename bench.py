@@ -48,6 +48,8 @@ WORKLOADS = {
     "sk24_ais": dict(kind="ais", instances=64, n=24, temps=200, beta=2.0,
                      samples=1024, update="sequential"),
     # learned proposal vs plain PT, TTS(99%) (not an attempts/s line)
+    "lattice64_sparse": dict(kind="lattice", side=64, replicas=40,
+                             reads=100, tmin=1.0, tmax=3.5),
     "rbm_mnist": dict(kind="rbm", visible=784, hidden=128, state_size=100,
                       steps=1, tmin=1.0, tmax=1.0, parallel=False),
     "sk512_tts": dict(kind="pm1", n=512, replicas=64, reads=128, tmin=0.3,
@@ -624,6 +626,87 @@ def run_rbm_workload(args, w, rank, world):
     return 0
 
 
+def run_lattice_workload(args, w, rank, world):
+    """2-D Ising lattice of the reference's tutorial
+    (tutorials/ising_tutorial.py:175-242: open-boundary nearest-neighbour
+    couplings -1, no field, `ones` start, sequential sweeps) at 64 x 64 =
+    4096 spins: attempts/s of the sparse-row sweep, beside the dense plain
+    sweep on the same chains, and end to end through Solver."""
+    if rank != 0:
+        return 0
+    import torch
+    from pysa_gb300 import Instance, PTBatch, Solver, pack_spins
+    from pysa_gb300 import _lib
+    from pysa_gb300._lib import check, ref
+    from pysa_gb300.utils import lattice_adjacency
+    L = w["side"]
+    n, R, Rd = L * L, w["replicas"], w["reads"]
+    P = -lattice_adjacency(L, L)
+    J = P.astype(np.float32)
+    h = np.zeros(n, np.float32)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    out = {}
+    for name, kw in (("sparse", dict(sparse=True)),
+                     ("dense_plain", dict(kernel="plain"))):
+        b = PTBatch("ising", [Instance(J, h, ladder(w), Rd)], **kw)
+        b.set_states(pack_spins(np.ones((Rd, R, n), np.float32), "ising",
+                                b.words), None)
+        st = torch.cuda.current_stream().cuda_stream
+        o = _lib.Options(3, _lib.SEQUENTIAL, 1, 0, 0, 0, 0)
+        steps = args.steps if name == "sparse" else max(3, args.steps // 10)
+        for _ in range(args.warmup):
+            check(b.lib.pysa_gb_sweeps(ref(b.p), ref(b.s), ref(b.ws), ref(o),
+                                       1, st), "sweep")
+        ev = []
+        torch.cuda.synchronize()
+        for k in range(steps):
+            flush.fill_(float(k))  # L2 flush (256 MB), untimed
+            e0, e1 = (torch.cuda.Event(enable_timing=True),
+                      torch.cuda.Event(enable_timing=True))
+            e0.record()
+            check(b.lib.pysa_gb_sweeps(ref(b.p), ref(b.s), ref(b.ws), ref(o),
+                                       1, st), "sweep")
+            e1.record()
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        b.check_status()
+        ms = sum(a.elapsed_time(c) for a, c in ev) / steps
+        out[name] = {"ms_per_sweep": ms, "attempts_per_s": Rd * R * n / ms
+                     * 1e3, "sweeps": steps,
+                     "best_energy": float(b.best_energy.min().item())}
+    # end to end: Solver with host buffers, sparse rows chosen by 'auto'
+    sv = Solver(P, "ising", "float32")
+    sv.metropolis_update(num_sweeps=2, num_reads=Rd, num_replicas=R,
+                         min_temp=w["tmin"], max_temp=w["tmax"],
+                         initialize_strategy="ones", sparse="auto", seed=1)
+    torch.cuda.synchronize()
+    e2e_sweeps = 200
+    t0 = time.perf_counter()
+    fr = sv.metropolis_update(num_sweeps=e2e_sweeps, num_reads=Rd,
+                              num_replicas=R, min_temp=w["tmin"],
+                              max_temp=w["tmax"], initialize_strategy="ones",
+                              sparse="auto", seed=2, return_dataframe=False)
+    dt = time.perf_counter() - t0
+    words = (n + 31) // 32
+    print(json.dumps({
+        "metric": "spin_flip_attempts_per_s",
+        "value": out["sparse"]["attempts_per_s"], "unit": "attempts/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": out["sparse"]["ms_per_sweep"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "the tutorial's lattice (deterministic)",
+        "config": {"workload": args.workload, **w, "n": n,
+                   "l2": "flushed (256 MB write) before every timed sweep"},
+        "kernels": out,
+        "e2e": {"value": Rd * R * n * e2e_sweeps / dt, "unit": "attempts/s",
+                "h2d_bytes_per_step": n * n * 4 + Rd * R * words * 4,
+                "d2h_bytes_per_step": Rd * R * (2 * words * 4 + 16),
+                "sweeps_per_call": e2e_sweeps, "seconds": dt,
+                "best_energy_min": float(min(r["best_energy"] for r in fr))},
+        "gpu_launches": 2 * args.steps}), flush=True)
+    return 0
+
+
 def _reference_sample(w):
     """(ptype, P, description) of the instance the reference arm times."""
     if w["kind"] == "sk_batch":
@@ -633,6 +716,11 @@ def _reference_sample(w):
         w2 = dict(w, kind="sk", n=n)
         ptype, P = make_instance(w2)
         return ptype, P, w2, f"median-size instance of the batch (n={n})"
+    if w["kind"] == "lattice":
+        from pysa_gb300.utils import lattice_adjacency
+        L = w["side"]
+        return ("ising", -lattice_adjacency(L, L).astype(np.float32),
+                dict(w, n=L * L), f"the {L} x {L} lattice")
     ptype, P = make_instance(w)
     return ptype, P, w, "the workload's instance"
 
@@ -748,6 +836,8 @@ def main():
                                   "GPU arm's line instead"}))
             return 0
         return run_rbm_workload(args, w, rank, world)
+    if w["kind"] == "lattice" and args.impl != "reference":
+        return run_lattice_workload(args, w, rank, world)
     if w["kind"] in ("sk_batch", "ais") and args.impl != "reference":
         fn = run_batch_workload if w["kind"] == "sk_batch" else run_ais_workload
         return fn(args, w, rank, world)

@@ -89,6 +89,18 @@ typedef struct {
   const float *h;           /* local fields = diagonal of the problem */
   const float *ladder;      /* inverse temperatures, slot order */
   const int32_t *ladder_sorted; /* per instance: argsort of its R betas */
+  /* sparse rows of the instances flagged in pysa_gb_host_tables.sparse
+   * (all NULL when none is).  Row i of instance k (row i of the transposed
+   * couplings above, as every kernel reads them) has its nonzero entries
+   * grouped by column % 8, ascending column inside a group; group g is
+   * entries csr_rows[9 (csr_row_off[k] + i) + g] ..
+   * csr_rows[9 (csr_row_off[k] + i) + g + 1] - 1, counted from the
+   * instance's first entry csr_ent_off[k]. */
+  const int64_t *csr_row_off; /* [num_instances] first row record (-1 dense) */
+  const int64_t *csr_ent_off; /* [num_instances] first entry */
+  const int32_t *csr_rows;    /* 9 int32 per row */
+  const int32_t *csr_col;     /* column of each entry */
+  const float *csr_val;       /* coupling of each entry */
 } pysa_gb_problems;
 
 /* Chain state, updated in place by the sweeps. */
@@ -154,6 +166,18 @@ typedef struct {
                                instance's tiles and diagonal blocks, -1 for
                                plain-kernel instances */
   int32_t tc_rand_slots;
+  /* host, from pysa_gb_setup: work items of the sparse-row sweep (one per
+   * csr_chains chains of each sparse instance) within items */
+  int32_t csr_item_start;
+  int32_t csr_item_count;
+  /* caller: 0 = the sparse tables are grouped rows (csr_rows); 4, 8, 16 or
+   * 32 = every sparse row is a fixed record of that many entries at
+   * csr_ent_off + width * i (csr_rows unused): the row's entries in the
+   * same group order, bit 31 of csr_col set on the last entry of each
+   * group, padding entries with value 0 */
+  int32_t csr_width;
+  int32_t csr_chains;     /* host, from pysa_gb_setup: chains per work item
+                             (128, or 64 / 32 while that leaves SMs idle) */
   int32_t pad_;
 } pysa_gb_workspace;
 
@@ -165,6 +189,9 @@ typedef struct {
   const int64_t *chain_off;
   const int64_t *j_off;
   const int32_t *ld;
+  const int32_t *sparse;  /* [num_instances] 1: the instance sweeps on the
+                             sparse-row kernel (pysa_gb_problems.csr_*);
+                             NULL: none does */
 } pysa_gb_host_tables;
 
 typedef struct {

@@ -26,7 +26,9 @@ class Problems(ctypes.Structure):
                 ("n", P), ("replicas", P), ("reads", P), ("j_off", P),
                 ("ld", P), ("h_off", P), ("chain_off", P), ("read_off", P),
                 ("ladder_off", P), ("read_inst", P), ("J", P), ("h", P),
-                ("ladder", P), ("ladder_sorted", P)]
+                ("ladder", P), ("ladder_sorted", P), ("csr_row_off", P),
+                ("csr_ent_off", P), ("csr_rows", P), ("csr_col", P),
+                ("csr_val", P)]
 
 
 class State(ctypes.Structure):
@@ -49,12 +51,14 @@ class Workspace(ctypes.Structure):
                 ("tc_fusable", I32), ("tc_sched", P), ("tc_unit_sweeps", I32),
                 ("tc_launch_sweeps", I32), ("tc_b_rand", P),
                 ("tc_diag_rand", P), ("tc_inst_off", P),
-                ("tc_rand_slots", I32), ("pad_", I32)]
+                ("tc_rand_slots", I32), ("csr_item_start", I32),
+                ("csr_item_count", I32), ("csr_width", I32),
+                ("csr_chains", I32), ("pad_", I32)]
 
 
 class HostTables(ctypes.Structure):
     _fields_ = [("n", P), ("replicas", P), ("reads", P), ("chain_off", P),
-                ("j_off", P), ("ld", P)]
+                ("j_off", P), ("ld", P), ("sparse", P)]
 
 
 class Options(ctypes.Structure):

@@ -22,7 +22,8 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
 SOURCES = ["abi.cu", "kernels_aux.cu", "plain_small.cu", "plain_large.cu",
-           "ais.cu", "sweep_tc.cu", "noalloc.cu", "gemm_tc.cu", "mlp.cu"]
+           "ais.cu", "sweep_tc.cu", "sweep_csr.cu", "noalloc.cu", "gemm_tc.cu",
+           "mlp.cu"]
 
 
 def _deps():

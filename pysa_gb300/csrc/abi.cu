@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "ais_api.h"
+#include "csr_api.h"
 #include "tc_api.h"
 #include "aux.cuh"
 #include "plain_variants.h"
@@ -68,6 +69,10 @@ static int cuda_fail(cudaError_t e, const char* where) {
 constexpr int kMaxFusedSweeps = 64;
 
 // Streaming multiprocessors of the current device (cached per device).
+static inline bool is_sparse(const pysa_gb_host_tables* h, int i) {
+  return h && h->sparse && h->sparse[i];
+}
+
 static int sm_count() {
   static int cache[64] = {};
   int dev = 0;
@@ -150,10 +155,16 @@ int pysa_gb_workspace_bytes(int32_t num_instances,
     if (replicas_host[i] < 1 || replicas_host[i] > kMaxReplicas)
       return fail(PYSA_GB_ERR_SIZE, "replicas must be in [1, 512]");
     if (reads_host[i] < 0) return fail(PYSA_GB_ERR_ARG, "negative reads");
+    const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
+    if (is_sparse(host, i)) {  // sparse-row sweep: fields only for prepare
+      items += (chains + 31) / 32;  // items of 32 chains at the smallest
+      const int nc = (n + 31) / 32;
+      if (nc > max_nc) max_nc = nc;
+      continue;
+    }
     const int v = plain_variant_for(n);
     const PlainVariant& pv = plain_variant(v);
     packed += (int64_t)n * row_floats(v);
-    const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
     const int cpb = pv.gw * pv.w;
     items += (chains + cpb - 1) / cpb;
     if (pv.nc > max_nc) max_nc = pv.nc;
@@ -192,14 +203,15 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   int64_t off = 0;
   for (int i = 0; i < p->num_instances; ++i) {
     poff[i] = off;
-    off += (int64_t)n_host[i] * row_floats(plain_variant_for(n_host[i]));
+    if (!is_sparse(host, i))
+      off += (int64_t)n_host[i] * row_floats(plain_variant_for(n_host[i]));
   }
   for (int v = 0; v < kNumPlainVariants; ++v) {
     ws->variant_start[v] = (int32_t)items.size();
     const PlainVariant& pv = plain_variant(v);
     const int cpb = pv.gw * pv.w;
     for (int i = 0; i < p->num_instances; ++i) {
-      if (plain_variant_for(n_host[i]) != v) continue;
+      if (is_sparse(host, i) || plain_variant_for(n_host[i]) != v) continue;
       const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
       for (int64_t c = 0; c < chains; c += cpb) {
         SweepItem it;
@@ -215,6 +227,40 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     }
     ws->variant_count[v] = (int32_t)items.size() - ws->variant_start[v];
   }
+  // sparse instances: up to 128 chains per item of the sparse-row sweep,
+  // fewer while the items would leave SMs idle
+  ws->csr_item_start = (int32_t)items.size();
+  int cpb = kCsrChains;
+  {
+    int64_t sparse_chains = 0;
+    for (int i = 0; i < p->num_instances; ++i)
+      if (is_sparse(host, i))
+        sparse_chains += (int64_t)replicas_host[i] * reads_host[i];
+    const int sms = sm_count();
+    while (cpb > 32 && (sparse_chains + cpb - 1) / cpb < sms) cpb /= 2;
+  }
+  ws->csr_chains = cpb;
+  for (int i = 0; i < p->num_instances; ++i) {
+    if (!is_sparse(host, i)) continue;
+    if (!p->csr_row_off || !p->csr_ent_off || !p->csr_col || !p->csr_val ||
+        (ws->csr_width == 0 && !p->csr_rows))
+      return fail(PYSA_GB_ERR_ARG, "sparse instance without csr tables");
+    if (ws->csr_width != 0 && ws->csr_width != 4 && ws->csr_width != 8 &&
+        ws->csr_width != 16 && ws->csr_width != 32)
+      return fail(PYSA_GB_ERR_ARG, "csr_width must be 0, 4, 8, 16 or 32");
+    const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
+    for (int64_t c = 0; c < chains; c += cpb) {
+      SweepItem it;
+      it.inst = i;
+      it.chain0 = (int32_t)(chain_off_host[i] + c);
+      it.nchains = (int32_t)((chains - c) < cpb ? (chains - c) : cpb);
+      it.variant = -1;
+      it.poff_lo = it.poff_hi = 0;
+      it.pad0 = it.pad1 = 0;
+      items.push_back(it);
+    }
+  }
+  ws->csr_item_count = (int32_t)items.size() - ws->csr_item_start;
   if (!items.empty()) {
     cudaError_t e = cudaMemcpyAsync(ws->items, items.data(),
                                     items.size() * sizeof(SweepItem),
@@ -223,9 +269,10 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   }
   // couplings into the packed row layout, per instance
   for (int i = 0; i < p->num_instances; ++i) {
-    const int v = plain_variant_for(n_host[i]);
     if (host->ld[i] < n_host[i])
       return fail(PYSA_GB_ERR_ARG, "ld < n");
+    if (is_sparse(host, i)) continue;
+    const int v = plain_variant_for(n_host[i]);
     launch_pack_rows(p->J + host->j_off[i], host->ld[i], n_host[i],
                      plain_variant(v).nc, lane_stride(v),
                      ws->packed_j + poff[i], st);
@@ -235,8 +282,10 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   return PYSA_GB_OK;
 }
 
-static inline bool tc_selected(int n, int min_n) {
-  return n >= (min_n < 64 ? 64 : min_n) && n <= 2048;
+static inline bool tc_selected(const pysa_gb_host_tables* host, int i,
+                               int min_n) {
+  const int n = host->n[i];
+  return !is_sparse(host, i) && n >= (min_n < 64 ? 64 : min_n) && n <= 2048;
 }
 
 // Chains per tensor-core work item of every selected instance: a CTA's full
@@ -249,7 +298,7 @@ static std::vector<int> tc_item_sizes(int num_instances,
                                       int min_n) {
   std::vector<int> size(num_instances, 0), gran(num_instances, 32);
   for (int i = 0; i < num_instances; ++i) {
-    if (!tc_selected(host->n[i], min_n)) continue;
+    if (!tc_selected(host, i, min_n)) continue;
     size[i] = tc_chains_per_cta(host->n[i]);
     if (size[i] % host->replicas[i] == 0) gran[i] = host->replicas[i];
   }
@@ -287,7 +336,7 @@ int pysa_gb_tc_workspace(int32_t num_instances,
   int64_t b = 0, d = 0, items = 0;
   for (int i = 0; i < num_instances; ++i) {
     const int n = host->n[i];
-    if (!tc_selected(n, min_n)) continue;
+    if (!tc_selected(host, i, min_n)) continue;
     b += tc_b_elems(n, terms);
     d += tc_diag_elems(n);
     const int64_t chains = (int64_t)host->replicas[i] * host->reads[i];
@@ -321,8 +370,8 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   for (int i = 0; i < p->num_instances; ++i) {
     boff[i] = bo;
     doff[i] = dd;
-    if (!tc_selected(host->n[i], min_n)) {
-      live |= 1 << plan.variant_of(host->n[i]);
+    if (!tc_selected(host, i, min_n)) {
+      if (!is_sparse(host, i)) live |= 1 << plan.variant_of(host->n[i]);
       continue;
     }
     if (tc_chains_per_cta(host->n[i]) % host->replicas[i] != 0) fusable = 0;
@@ -518,6 +567,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   // (or none), no log-omega; several sweeps per launch with the fields
   // resident in tensor memory.
   const bool fused = use_tc && phases == 3 && ws->plain_live == 0 &&
+                     ws->csr_item_count == 0 &&
                      o->log_omega_stride == 0 &&
                      (!o->use_pt || ws->tc_fusable) && ws->tc_sched;
   // random order on the tensor cores: visiting orders of the next `cnt`
@@ -570,6 +620,21 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
       const int grid = count < caps[v] ? count : caps[v];
       cudaError_t e = plain_variant(v).launch(a, random, grid, st);
       if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+    }
+    if ((phases & 1) && ws->csr_item_count > 0) {
+      CsrArgs ca;
+      ca.p = *p;
+      ca.s = *s;
+      ca.perm = ws->perm;
+      ca.perm_slots = a.perm_slots;
+      ca.num_items = ws->csr_item_count;
+      ca.items = reinterpret_cast<const SweepItem*>(ws->items) +
+                 ws->csr_item_start;
+      ca.seed = o->seed;
+      ca.width = ws->csr_width;
+      ca.chains = ws->csr_chains > 0 ? ws->csr_chains : kCsrChains;
+      cudaError_t e = launch_csr(ca, random, st);
+      if (e != cudaSuccess) return cuda_fail(e, "sparse sweep launch");
     }
     if (phases & 2) launch_exchange(x, st);
   }

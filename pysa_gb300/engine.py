@@ -47,6 +47,55 @@ def bf16_exact(a: np.ndarray) -> bool:
     return bool(np.all((u & 0xFFFF) == 0))
 
 
+def csr_tables(J: np.ndarray):
+    """Sparse-row tables of a dense coupling matrix, as the sparse-row sweep
+    reads them: row i of J^T (the row every kernel reads for spin i) keeps
+    its nonzero entries grouped by column % 8, ascending column inside a
+    group.  Returns rows [n, 9] int32 (group starts and the row end), col
+    int32 and val float32."""
+    Jt = np.ascontiguousarray(np.asarray(J, np.float32).T)
+    n = Jt.shape[0]
+    r, c = np.nonzero(Jt)
+    g = c & 7
+    order = np.lexsort((c, g, r))
+    r, c, g = r[order], c[order], g[order]
+    cnt = np.zeros(8 * n, np.int64)
+    np.add.at(cnt, 8 * r + g, 1)
+    starts = np.concatenate([[0], np.cumsum(cnt)])
+    rows = starts[8 * np.arange(n)[:, None] + np.arange(9)[None, :]]
+    return (rows.astype(np.int32), c.astype(np.int32),
+            Jt[r, c].astype(np.float32))
+
+
+def csr_records(J: np.ndarray, width: int):
+    """Fixed-width sparse rows: row i of J^T as `width` entries in the order
+    of csr_tables (grouped by column % 8), bit 31 of the column set on the
+    last entry of each group, padding entries (column i, value 0) flagged
+    last.  Returns col [n, width] int32 and val [n, width] float32."""
+    rows, col, val = csr_tables(J)
+    n = rows.shape[0]
+    deg = (rows[:, 8] - rows[:, 0]).astype(np.int64)
+    if n and deg.max() > width:
+        raise ValueError("a row has more entries than the record width")
+    k = np.arange(width)[None, :]
+    live = k < deg[:, None]
+    e = np.where(live, rows[:, :1].astype(np.int64) + k, 0)
+    c = np.where(live, col[e] if len(col) else 0,
+                 np.arange(n)[:, None]).astype(np.int64)
+    v = np.where(live, val[e] if len(val) else 0.0, 0.0).astype(np.float32)
+    nxt_live = np.concatenate([live[:, 1:], np.zeros((n, 1), bool)], axis=1)
+    nxt_grp = np.concatenate([c[:, 1:] & 7, np.full((n, 1), -1)], axis=1)
+    last = ~live | ~nxt_live | (nxt_grp != (c & 7))
+    c = c | (last.astype(np.int64) << 31)
+    return (c & 0xFFFFFFFF).astype(np.uint32).view(np.int32), v
+
+
+def mean_degree(J: np.ndarray) -> float:
+    """Nonzero couplings per row."""
+    J = np.asarray(J)
+    return float(np.count_nonzero(J)) / max(J.shape[0], 1)
+
+
 def _ptr(t: torch.Tensor) -> int:
     return t.data_ptr() if t is not None and t.numel() > 0 else 0
 
@@ -64,7 +113,7 @@ class PTBatch:
     def __init__(self, problem_type: str, instances: list[Instance],
                  device: torch.device | str | None = None,
                  perm_slots: int = 1, kernel: str = "auto",
-                 tc_terms: int | None = None):
+                 tc_terms: int | None = None, sparse=None):
         """kernel: 'plain' (CUDA-core sweep for every instance), 'tc'
         (tensor-core blocked sweep for every instance, sequential order,
         64 <= n <= 2048), 'auto' (tensor cores for the instances with
@@ -73,7 +122,11 @@ class PTBatch:
         timing; run() calls it on first use).  tc_terms sizes the
         tensor-core tiles for 1 or 2 BF16 terms (default: 1 when every J is
         exactly BF16); load_problem() needs room for 2 when later couplings
-        may not be."""
+        may not be.  sparse: instances that sweep on the sparse-row kernel
+        (field of spin i from row i's nonzero couplings, O(degree) per
+        attempt): None / False for none, True for all, 'auto' for those
+        whose mean degree is at most max(8, n / 64), or one bool per
+        instance."""
         if not torch.cuda.is_available():
             raise RuntimeError(
                 "pysa_gb300 needs a CUDA GPU: the sweeps run only as "
@@ -125,6 +178,46 @@ class PTBatch:
                 np.asarray(x.ladder, np.float32), kind="stable")
         read_inst = np.repeat(np.arange(I, dtype=np.int32), Rd)
         dev = self.device
+        # sparse-row instances and their tables
+        if sparse is None or sparse is False:
+            flags = [False] * I
+        elif sparse is True:
+            flags = [True] * I
+        elif sparse == "auto":
+            flags = [mean_degree(x.J) <= max(8.0, len(x.h) / 64)
+                     for x in instances]
+        else:
+            flags = [bool(f) for f in sparse]
+            if len(flags) != I:
+                raise ValueError("sparse: one flag per instance")
+        self.sparse = np.asarray(flags, np.int32) if I else np.zeros(
+            1, np.int32)
+        row_off = np.full(max(I, 1), -1, np.int64)
+        ent_off = np.zeros(max(I, 1), np.int64)
+        rows_l, col_l, val_l = [], [], []
+        nr, ne = 0, 0
+        # fixed records when every sparse row has at most 32 entries
+        maxdeg = max([int(np.count_nonzero(x.J, axis=0).max(initial=0))
+                      for i, x in enumerate(instances) if flags[i]] or [0])
+        self.csr_width = next((w for w in (4, 8, 16, 32) if maxdeg <= w), 0)
+        for i, x in enumerate(instances):
+            if not flags[i]:
+                continue
+            row_off[i], ent_off[i] = nr, ne
+            if self.csr_width:
+                cc, vv = csr_records(x.J, self.csr_width)
+                col_l.append(cc.ravel())
+                val_l.append(vv.ravel())
+                nr += cc.shape[0]
+                ne += cc.size
+            else:
+                rw, cc, vv = csr_tables(x.J)
+                rows_l.append(rw)
+                col_l.append(cc)
+                val_l.append(vv)
+                nr += rw.shape[0]
+                ne += cc.shape[0]
+        self.has_sparse = any(flags)
 
         def T(a):
             return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
@@ -134,6 +227,15 @@ class PTBatch:
                        read_off=T(read_off), ladder_off=T(ladder_off),
                        read_inst=T(read_inst if rt else np.zeros(1, np.int32)),
                        J=T(Jcat), h=T(hcat), ladder=T(lad), lsort=T(lsort))
+        if self.has_sparse:
+            self._t.update(
+                csr_row_off=T(row_off), csr_ent_off=T(ent_off),
+                csr_rows=T(np.concatenate(rows_l) if rows_l else
+                           np.zeros(9, np.int32)),
+                csr_col=T(np.concatenate(col_l) if ne else
+                          np.zeros(1, np.int32)),
+                csr_val=T(np.concatenate(val_l) if ne else
+                          np.zeros(1, np.float32)))
         t = self._t
         self.p = _lib.Problems(
             self.ptype, I, self.max_n, self.words, ct, rt, _ptr(t["n"]),
@@ -141,6 +243,10 @@ class PTBatch:
             _ptr(t["h_off"]), _ptr(t["chain_off"]), _ptr(t["read_off"]),
             _ptr(t["ladder_off"]), _ptr(t["read_inst"]), _ptr(t["J"]),
             _ptr(t["h"]), _ptr(t["ladder"]), _ptr(t["lsort"]))
+        if self.has_sparse:
+            for k in ("csr_row_off", "csr_ent_off", "csr_rows", "csr_col",
+                      "csr_val"):
+                setattr(self.p, k, _ptr(t[k]))
         C, W = max(ct, 1), self.words
         z = lambda *s, dt: torch.zeros(*s, dtype=dt, device=dev)  # noqa: E731
         self.spins = z(C, W, dt=torch.int32)
@@ -160,7 +266,7 @@ class PTBatch:
                             _ptr(self.best_spins), 0, _ptr(self.sweep_counter),
                             _ptr(self.status), _ptr(self.ticket))
         # workspace
-        self._host = (n, R, Rd, chain_off, j_off, ld)
+        self._host = (n, R, Rd, chain_off, j_off, ld, self.sparse)
         ht_ = _lib.HostTables(*(a.ctypes.data for a in self._host))
         need = (ctypes.c_int64 * 3)()
         items = check(self.lib.pysa_gb_workspace_bytes(I, ref(ht_), need),
@@ -175,6 +281,7 @@ class PTBatch:
                                  self.perm_slots, _ptr(self.perm),
                                  _ptr(self.packed_j), int(need[0]),
                                  _ptr(self.items), max(items, 1))
+        self.ws.csr_width = self.csr_width
         self._stream = torch.cuda.current_stream(dev)
         check(self.lib.pysa_gb_setup(ref(self.p), ref(ht_), ref(self.ws),
                                      self._stream.cuda_stream), "setup")
@@ -182,13 +289,17 @@ class PTBatch:
         self._ht = ht_
         self.tc = False
         self.tc_min_n = None
+        dense_tc = (n >= 64) & (n <= 2048) & (self.sparse[:I] == 0)
         if kernel == "tc":
-            if I and (n.min() < 64 or n.max() > 2048):
+            dense = self.sparse[:I] == 0
+            if I and dense.any() and (n[dense].min() < 64 or
+                                      n[dense].max() > 2048):
                 raise ValueError("kernel='tc' needs 64 <= n <= 2048 for "
-                                 "every instance")
-            self._setup_tc(64)
+                                 "every dense instance")
+            if dense_tc.any():
+                self._setup_tc(64)
         elif kernel in ("auto", "autotune"):
-            if I and ((n >= 64) & (n <= 2048)).any():
+            if I and dense_tc.any():
                 self._setup_tc(64)
         elif kernel != "plain":
             raise ValueError(f"unknown kernel {kernel!r}")
@@ -206,7 +317,9 @@ class PTBatch:
         ht_ = self._ht
         if not hasattr(self, "tc_b"):
             # sized once for the widest selection (every instance >= 64)
-            terms = 1 if all(bf16_exact(x.J) for x in self.instances) else 2
+            terms = 1 if all(bf16_exact(x.J) for i, x in
+                             enumerate(self.instances)
+                             if not self.sparse[i]) else 2
             if self._tc_terms_req is not None:
                 terms = max(terms, int(self._tc_terms_req))
             tneed = (ctypes.c_int64 * 3)()

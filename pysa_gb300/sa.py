@@ -150,13 +150,16 @@ class Solver(object):
                           verbose: bool = False,
                           get_part_fun: bool = False,
                           beta0: bool = False,
-                          seed: int = None):
+                          seed: int = None,
+                          sparse=None):
         """Parallel-tempering Metropolis run (pysa/sa.py:92-430).
 
         Returns one row per read with the reference's columns: 'states',
         'energies', 'best_state', 'best_energy', 'temps', ['log_Zf'],
         'num_sweeps', 'min_sweeps', 'init_time (us)', 'runtime (us)',
-        'problem_type', 'float_type'.  `seed` keys the GPU random stream.
+        'problem_type', 'float_type'.  `seed` keys the GPU random stream;
+        `sparse` (None, True or 'auto') sends the sweeps to the sparse-row
+        kernel, whose cost per attempt follows the row's nonzero couplings.
         """
         if send_background:  # pysa/sa.py:140-142
             kw = dict(locals())
@@ -280,7 +283,7 @@ class Solver(object):
             Instance(np.asarray(couplings, np.float32),
                      np.asarray(local_fields, np.float32),
                      np.asarray(betas, np.float32), Rd)
-        ])
+        ], sparse=sparse)
         words = batch.words
         e0 = None if energies_given is None else np.tile(
             np.asarray(energies_given, np.float32), Rd)

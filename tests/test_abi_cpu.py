@@ -27,7 +27,7 @@ def test_library_exports_every_header_symbol():
 
 def test_struct_sizes_match_header_layout():
     from pysa_gb300 import _lib
-    assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 14 * 8
+    assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 19 * 8
     assert ctypes.sizeof(_lib.State) == 11 * 8
     assert ctypes.sizeof(_lib.Options) == 8 + 6 * 4
     assert ctypes.sizeof(_lib.AisOptions) == 8 + 4 * 4 + 8 + 2 * 4
@@ -37,7 +37,7 @@ def _tables(n, R, Rd):
     from pysa_gb300 import _lib
     arrs = [np.asarray(n, np.int32), np.asarray(R, np.int32),
             np.asarray(Rd, np.int32)]
-    return arrs, _lib.HostTables(*(a.ctypes.data for a in arrs), 0, 0, 0)
+    return arrs, _lib.HostTables(*(a.ctypes.data for a in arrs), 0, 0, 0, 0)
 
 
 def test_workspace_plan_host_only():
