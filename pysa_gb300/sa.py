@@ -30,6 +30,7 @@ from typing import Any, List
 import numpy as np
 
 from . import ais as _ais
+from . import tts as _tts
 from .engine import Instance, PTBatch, pack_spins, run_ais, unpack_spins
 
 Vector = List[float]
@@ -160,6 +161,8 @@ class Solver(object):
         'problem_type', 'float_type'.  `seed` keys the GPU random stream;
         `sparse` (None, True or 'auto') sends the sweeps to the sparse-row
         kernel, whose cost per attempt follows the row's nonzero couplings.
+        min_temp / max_temp may be 'auto': the temperature range of the
+        reference's HPO tutorial (pysa_gb300.tts.temperature_range).
         """
         if send_background:  # pysa/sa.py:140-142
             kw = dict(locals())
@@ -183,6 +186,19 @@ class Solver(object):
                 raise ValueError("len('init_energies') != 'num_replicas'.")
         if get_part_fun:
             beta0 = True
+        if min_temp == "auto" or max_temp == "auto":
+            # the HPO tutorial's range: the largest single-flip change
+            # accepted half the time at max_temp, the smallest one 1 % of
+            # the time (over its multiplicity) at min_temp
+            if self.problem_type == "qubo":
+                hot, cold, cnt = _tts.delta_e_qubo(
+                    self.couplings + np.diag(self.local_fields))
+            else:
+                hot, cold, cnt = _tts.delta_e_ising(self.couplings,
+                                                    self.local_fields)
+            lo, hi = _tts.temperature_range(hot, cold, cnt)
+            min_temp = lo if min_temp == "auto" else min_temp
+            max_temp = hi if max_temp == "auto" else max_temp
         # ladder, pysa/sa.py:167-201
         if temps is None:
             if not num_replicas:

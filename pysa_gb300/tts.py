@@ -88,3 +88,62 @@ def batch_tts(best_energy, target, t_batch: float, ptgt: float = 0.99,
     return {"success_prob": success.mean(1), "nts": n, "t_run": t_run,
             "tts": tts, "tts_median": med,
             "solved_instances": int(np.isfinite(tts).sum())}
+
+
+# ------------------------------------------------------------ HPO helpers
+# The temperature heuristics and objective of the reference's hyperparameter
+# tutorial (tutorials/hpo_demo.ipynb, cells "get_delta_e_ising",
+# "get_delta_e_qubo", the temperature range cell and "tts_objective_fcn").
+
+def delta_e_ising(J, h, scaling_correction: bool = True):
+    """(dE_hot, dE_cold, count_min) of an Ising problem with symmetric J and
+    field vector h: dE_hot = 2 max_i (sum_j |J_ij| + |h_i|), the largest
+    single-flip energy change; dE_cold = 2 min of the nonzero |J_ij|, |h_i|,
+    the smallest; count_min = how many spins have that smallest coupling as
+    their own smallest nonzero term (their |h_i| if nonzero, else their
+    smallest |J_ij|), or 1 without the scaling correction."""
+    J = np.asarray(J.toarray() if hasattr(J, "toarray") else J, np.float64)
+    h = np.asarray(h, np.float64).reshape(-1)
+    aJ, ah = np.abs(J), np.abs(h)
+    de_hot = 2.0 * float(np.max(aJ.sum(axis=1) + ah))
+    smallest = min(float(aJ[aJ != 0].min(initial=np.inf)),
+                   float(ah[ah != 0].min(initial=np.inf)))
+    row_min = np.where(aJ != 0, aJ, np.inf).min(axis=1)
+    own = np.where(ah != 0, ah, row_min)
+    count = int(np.sum(np.minimum(row_min, own) == smallest)) \
+        if scaling_correction else 1
+    return de_hot, 2.0 * smallest, count
+
+
+def delta_e_qubo(Q):
+    """delta_e_ising of the Ising form of a symmetric QUBO matrix Q
+    (x = (s + 1) / 2): J = offdiag(Q) / 4, h = (1^T Q) / 2."""
+    Q = np.asarray(Q.toarray() if hasattr(Q, "toarray") else Q, np.float64)
+    J = (Q - np.diag(np.diag(Q))) / 4.0
+    h = np.ones(Q.shape[0]) @ Q / 2.0
+    return delta_e_ising(J, h)
+
+
+def temperature_range(de_hot: float, de_cold: float, count_min: int = 1,
+                      p_hot: float = 0.5, p_cold: float = 0.01):
+    """(min_temp, max_temp) at which the smallest move is accepted with
+    probability p_cold / count_min and the largest with p_hot:
+    T = -dE / log(p)."""
+    max_temp = -de_hot / np.log(p_hot)
+    min_temp = -de_cold / np.log(p_cold / count_min)
+    return float(min_temp), float(max_temp)
+
+
+def tts_objective(energies, mean_runtime: float, gs_energy: float,
+                  s: float = 0.99, opt_gap: float = 0.05,
+                  fail_value: float = 1e10) -> float:
+    """Time to solution for tuning: success = energy within opt_gap of the
+    ground-state energy (E <= E_gs (1 - opt_gap)); mean_runtime when the
+    success rate reaches s, fail_value when it is 0, else
+    mean_runtime ln(1 - s) / ln(1 - p)."""
+    p = float(np.mean(np.asarray(energies) <= gs_energy * (1.0 - opt_gap)))
+    if p == 0.0:
+        return float(fail_value)
+    if p >= s:
+        return float(mean_runtime)
+    return float(mean_runtime * np.log(1.0 - s) / np.log(1.0 - p))

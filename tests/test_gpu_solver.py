@@ -142,3 +142,20 @@ def test_background_returns_future():
                               return_dataframe=False, seed=1)
     rows = fut.result(timeout=120)
     assert len(rows) == 2 and rows[0]["num_sweeps"] == 4
+
+
+def test_auto_temperature_range_on_wishart():
+    """min_temp / max_temp = 'auto' (the HPO tutorial's range) reaches the
+    planted Wishart N=50 ground state."""
+    from conftest import golden
+    from pysa_gb300 import Solver
+    from pysa_gb300.tts import delta_e_ising, temperature_range
+    g = golden("wishart50")
+    P = g["problem"]
+    res = Solver(P, "ising", "float32").metropolis_update(
+        num_sweeps=2000, num_reads=16, num_replicas=32, min_temp="auto",
+        max_temp="auto", seed=3, return_dataframe=False)
+    lo, hi = temperature_range(*delta_e_ising(P, np.zeros(P.shape[0])))
+    assert np.isclose(min(res[0]["temps"]), lo, rtol=1e-6)
+    assert np.isclose(max(res[0]["temps"]), hi, rtol=1e-6)
+    assert min(2 * r["best_energy"] for r in res) == g["ground_energy_x2"]

@@ -4,6 +4,7 @@ tests/golden/make_golden_tts.py."""
 import json
 
 import numpy as np
+import pytest
 
 from conftest import golden
 
@@ -37,3 +38,32 @@ def test_batch_tts_convention():
     assert np.isclose(r["tts"][0], r["t_run"] * np.log(0.01) / np.log(0.5))
     assert np.isinf(r["tts"][2])
     assert r["solved_instances"] == 2
+
+
+# ------------------------------------------------- HPO tutorial helpers
+@pytest.mark.parametrize("name", ["wishart", "ising_int", "ising_sparse"])
+def test_delta_e_and_temperature_range_match_reference(name):
+    from pysa_gb300.tts import delta_e_ising, temperature_range
+    g = golden("hpo")
+    J, h = g[f"{name}_J"], g[f"{name}_h"]
+    for sc in (1, 0):
+        got = delta_e_ising(J, h, bool(sc))
+        assert np.array_equal(np.array(got, float), g[f"{name}_{sc}"])
+    hot, cold, cnt = delta_e_ising(J, h)
+    assert np.allclose(temperature_range(hot, cold, cnt), g[f"{name}_range"],
+                       rtol=0, atol=0)
+
+
+def test_delta_e_qubo_matches_reference():
+    from pysa_gb300.tts import delta_e_qubo
+    g = golden("hpo")
+    assert np.array_equal(np.array(delta_e_qubo(g["qubo_Q"]), float),
+                          g["qubo"])
+
+
+def test_tts_objective_matches_reference():
+    from pysa_gb300.tts import tts_objective
+    g = golden("hpo")
+    got = [tts_objective(g["tts_energies"], 0.25, gs)
+           for gs in (-100.0, -110.0, -90.0, -200.0)]
+    assert np.array_equal(np.array(got), g["tts_objective"])
