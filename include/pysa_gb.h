@@ -217,7 +217,9 @@ const char *pysa_gb_last_error(void);
  * there: [0] decision start, [1] fields ready, [2] decisions done, [3] A free,
  * [4] A published, [5] MMA start, [6] next-block fields committed, [7] stages
  * issued, [8 + 3g .. 10 + 3g] sub-block g: fields loaded, lazy corrections
- * applied, decided.  NULL turns it off.  No counterpart in the reference. */
+ * applied, decided.  NULL turns it off.  Recorded only by builds with
+ * PYSA_GB_TRACE defined (PYSA_GB_TRACE=1 in the environment of the build
+ * script).  No counterpart in the reference. */
 int pysa_gb_set_trace(void *device_buffer);
 
 /* Workspace sizing and set-up.

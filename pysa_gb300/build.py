@@ -20,6 +20,8 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
+if os.environ.get("PYSA_GB_TRACE") == "1":  # timeline stamps (diagnostics)
+    FLAGS.append("-DPYSA_GB_TRACE")
 
 SOURCES = ["abi.cu", "kernels_aux.cu", "plain_small.cu", "plain_large.cu",
            "ais.cu", "sweep_tc.cu", "sweep_csr.cu", "noalloc.cu", "gemm_tc.cu",

@@ -98,15 +98,21 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
   }
 }
 
-// Timeline stamps of CTA 0 when a trace buffer is given (diagnostics only):
+// Timeline stamps of CTA 0 when a trace buffer is given, in builds with
+// PYSA_GB_TRACE defined (diagnostics only: the stamps' branches in the
+// decision loop cost about 8 % of a sweep, so release builds drop them):
 // row G < 48 per block, row 48 whole-unit marks (entry, set-up done, last
 // MMA done, fields stored, unit done, field load start; the last unit's).
 __device__ __forceinline__ void stamp(const TcArgs& a, uint32_t G, int slot) {
+#ifdef PYSA_GB_TRACE
   if (a.trace && blockIdx.x == 0 && G < 48)
     a.trace[G * 24 + slot] = globaltimer_ns();
+#endif
 }
 __device__ __forceinline__ void stamp_cta(const TcArgs& a, int slot) {
+#ifdef PYSA_GB_TRACE
   if (a.trace && blockIdx.x == 0) a.trace[48 * 24 + slot] = globaltimer_ns();
+#endif
 }
 
 // Named barriers in inline PTX: the warp is reconverged first and the
@@ -131,6 +137,107 @@ __device__ __forceinline__ void named_sync_helpers() {
 __device__ __forceinline__ uint32_t bf16_bits(float d) {
   // exact for d in {0, +-1, +-2}
   return __float_as_uint(d) >> 16;
+}
+
+// The rare exact redo of one deciding thread's sub-block (some decision of
+// the warp fell inside the f32 band), kept out of line: inlined, its code
+// and registers slow the fast path by about 12 %.  It rebuilds the
+// sub-block's fields exactly as the fast path does (same loads, same
+// correction order), decides every spin with the exact rule and writes the
+// deltas to dl_s; returns the new spin word and block energy change.
+struct RedoCtx {
+  const float* jb;          // diagonal block of the block, [64][64]
+  float* dl_s;              // deltas [64][CC]
+  const float* corr_s;      // helper corrections (fold 2)
+  const float* hbuf;        // gathered fields (random order, fold > 1)
+  const int32_t* perm_w;    // this warp's visiting positions (random order)
+  const float* lfb;         // log-uniforms [64][CC]
+  uint32_t taddr;           // TMEM address of the thread's lane
+  int co, kmax, c, g, i0, sb;
+  int valid, ising;
+  float beta;
+  uint64_t seed;
+  uint32_t inst, sweep, chain_local;
+  uint32_t wsave;           // spin word before the sub-block
+  float dEsave;
+};
+
+template <int F, bool RND>
+__device__ __noinline__ void redo_subblock(const RedoCtx& x, uint32_t* wcur,
+                                           float* dEb) {
+  constexpr int CC = 128 / F;
+  const int g = x.g, c = x.c;
+  float hs[16];
+  if constexpr (!RND) {
+    tc::tmem_ld16(x.taddr + x.co + 16 * g, hs);
+  } else if constexpr (F > 1) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      hs[j] = 16 * g + j < x.kmax ? x.hbuf[(16 * g + j) * CC + c] : 0.0f;
+  } else {
+    uint32_t r[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int sp = x.perm_w[16 * g + j];
+      r[j] = 0u;
+      if (sp >= 0) r[j] = tc::tmem_ld1_nowait(x.taddr + (uint32_t)sp);
+    }
+    tc::tmem_wait_ld16(r);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) hs[j] = __uint_as_float(r[j]);
+  }
+  const bool help = F == 2;
+  if (help && g >= 2) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) hs[j] += x.corr_s[((g - 2) * 16 + j) * CC + c];
+  }
+  for (int k = help && g >= 2 ? 16 * (g - 1) : 0; k < 16 * g; ++k) {
+    const float d = x.dl_s[k * CC + c];
+    const float4* jr = reinterpret_cast<const float4*>(x.jb + k * 64 + 16 * g);
+#pragma unroll
+    for (int q4 = 0; q4 < 4; ++q4) {
+      const float4 v = jr[q4];
+      hs[4 * q4 + 0] = fmaf(d, v.x, hs[4 * q4 + 0]);
+      hs[4 * q4 + 1] = fmaf(d, v.y, hs[4 * q4 + 1]);
+      hs[4 * q4 + 2] = fmaf(d, v.z, hs[4 * q4 + 2]);
+      hs[4 * q4 + 3] = fmaf(d, v.w, hs[4 * q4 + 3]);
+    }
+  }
+  uint32_t w = x.wsave;
+  float e = x.dEsave;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int k = 16 * g + j;
+    const bool sbit = (w >> (x.sb + j)) & 1u;
+    const float hk = hs[j];
+    const float dn =
+        x.ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
+    const bool acc = x.valid && k < x.kmax &&
+                     metropolis_accept_lf(dn, x.beta, x.lfb[k * CC + c],
+                                          x.seed, x.inst, x.sweep,
+                                          x.chain_local, (uint32_t)(x.i0 + k));
+    const float dl =
+        acc ? (x.ising ? (sbit ? -2.0f : 2.0f) : (sbit ? -1.0f : 1.0f)) : 0.0f;
+    x.dl_s[k * CC + c] = dl;
+    if (acc) {
+      e -= dn;
+      w ^= 1u << (x.sb + j);
+    }
+    if (j < 15) {
+      const float4* jr =
+          reinterpret_cast<const float4*>(x.jb + k * 64 + 16 * g);
+#pragma unroll
+      for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
+        const float4 v = jr[q4];
+        if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
+        if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
+        if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
+        if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
+      }
+    }
+  }
+  *wcur = w;
+  *dEb = e;
 }
 
 // Work units: unit u is item u % num_items for sweeps
@@ -544,7 +651,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             float dprev[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) dprev[j] = 0.0f;
-            bool a_ok = true;
+            bool a_early = false;
             // one sub-block's deltas into the A rows of every slice
             auto put_a = [&](int gg, const float* d) {
               uint32_t pkg[8];
@@ -563,9 +670,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
             };
             // fields of sub-block g with the corrections of every earlier
-            // sub-block of the block (again = a redo: the fields are read
-            // once more)
-            auto fields = [&](int g, bool again, float* hs) {
+            // sub-block of the block
+            auto fields = [&](int g, float* hs) {
               if constexpr (!RND) {
                 tc::tmem_ld16(taddr + lane_base + co + 16 * g, hs);
               } else if constexpr (F > 1) {
@@ -587,7 +693,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) hs[j] = __uint_as_float(r[j]);
               }
-              if (lead && !again) stamp(a, Gb, 8 + 3 * g);
+              if (lead) stamp(a, Gb, 8 + 3 * g);
               // sub-blocks before the previous one: precomputed by the
               // helpers (fold 2) or from the deltas in shared memory
               if (C::HELP && g >= 2) {
@@ -632,7 +738,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     #pragma unroll 1
             for (int g = 0; g < 4; ++g) {
               float hs[16];
-              fields(g, false, hs);
+              fields(g, hs);
               if (lead) stamp(a, Gb, 9 + 3 * g);
               uint32_t wcur = g < 2 ? w0 : w1;
               const int sb = 16 * (g & 1);
@@ -682,57 +788,45 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 }
               }
               if (__any_sync(0xffffffffu, unc)) {
-                // rare: redo the sub-block with the exact f64 rule where
-                // needed, from freshly rebuilt fields
-                wcur = wsave;
-                dEb = dEsave;
-                fields(g, true, hs);
-    #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                  const int k = 16 * g + j;
-                  const bool sbit = (wcur >> (sb + j)) & 1u;
-                  const float hk = hs[j];
-                  const float dn =
-                      ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
-                  const bool acc =
-                      valid && k < kmax &&
-                      metropolis_accept_lf(dn, beta, lfv[j], a.seed,
-                                           (uint32_t)inst, sweep, chain_local,
-                                           (uint32_t)(i0 + k));
-                  const float dl = acc ? (ising ? (sbit ? -2.0f : 2.0f)
-                                                : (sbit ? -1.0f : 1.0f))
-                                       : 0.0f;
-                  dcur[j] = dl;
-                  if (acc) {
-                    dEb -= dn;
-                    wcur ^= 1u << (sb + j);
-                  }
-                  if (j < 15) {
-                    const float4* jr =
-                        reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
-    #pragma unroll
-                    for (int q4 = (j + 1) >> 2; q4 < 4; ++q4) {
-                      const float4 v = jr[q4];
-                      if (4 * q4 + 0 > j) hs[4 * q4 + 0] = fmaf(dl, v.x, hs[4 * q4 + 0]);
-                      if (4 * q4 + 1 > j) hs[4 * q4 + 1] = fmaf(dl, v.y, hs[4 * q4 + 1]);
-                      if (4 * q4 + 2 > j) hs[4 * q4 + 2] = fmaf(dl, v.z, hs[4 * q4 + 2]);
-                      if (4 * q4 + 3 > j) hs[4 * q4 + 3] = fmaf(dl, v.w, hs[4 * q4 + 3]);
-                    }
-                  }
-                }
+                // rare: the whole sub-block again with the exact f64 rule
+                // where needed (out of line)
+                RedoCtx rx;
+                rx.jb = jb;
+                rx.dl_s = dl_s;
+                rx.corr_s = corr_s;
+                rx.hbuf = hbuf;
+                rx.perm_w = perm_s + warp * 64;
+                rx.lfb = lfb;
+                rx.taddr = taddr + lane_base;
+                rx.co = co;
+                rx.kmax = kmax;
+                rx.c = c;
+                rx.g = g;
+                rx.i0 = i0;
+                rx.sb = sb;
+                rx.valid = valid;
+                rx.ising = ising;
+                rx.beta = beta;
+                rx.seed = a.seed;
+                rx.inst = (uint32_t)inst;
+                rx.sweep = sweep;
+                rx.chain_local = chain_local;
+                rx.wsave = wsave;
+                rx.dEsave = dEsave;
+                redo_subblock<F, RND>(rx, &wcur, &dEb);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) dcur[j] = dl_s[(16 * g + j) * CC + c];
               }
               if (g < 2) w0 = wcur; else w1 = wcur;
 #pragma unroll
               for (int j = 0; j < 16; ++j) dl_s[(16 * g + j) * CC + c] = dcur[j];
               // deltas into the A rows.  A is single-buffered: the previous
-              // block's MMAs must be done first; waiting after the second
-              // sub-block leaves them that long to finish
-              if (g == 1 && Gb > G0) {
-                if (lead) stamp(a, Gb, 2);
-                a_ok = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
-                if (lead) stamp(a, Gb, 3);
-              }
-              if (a_ok && g >= 1) {
+              // block's MMAs must be done first.  After the second sub-block
+              // they usually are (one slice's worth of MMAs); if not (long
+              // MMAs at fold 4), the rows wait for the block's end
+              if (g == 1)
+                a_early = Gb == G0 || mbar_test_wait(sh.mma_done, (Gb - 1) & 1);
+              if (a_early && g >= 1) {
                 if (g == 1) put_a(0, dprev);
                 put_a(g, dcur);
               }
@@ -740,6 +834,24 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               for (int j = 0; j < 16; ++j) dprev[j] = dcur[j];
               if (lead) stamp(a, Gb, 10 + 3 * g);
               if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
+            }
+            if (!a_early) {
+              if (Gb > G0) {
+                if (lead) stamp(a, Gb, 2);
+                const bool a_ok =
+                    tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
+                if (lead) stamp(a, Gb, 3);
+                if (!a_ok) a_early = true;  // aborting: leave A alone
+              }
+              if (!a_early) {
+    #pragma unroll 1
+                for (int gg = 0; gg < 4; ++gg) {
+                  float d[16];
+#pragma unroll
+                  for (int j = 0; j < 16; ++j) d[j] = dl_s[(16 * gg + j) * CC + c];
+                  put_a(gg, d);
+                }
+              }
             }
             if (valid) {
               if constexpr (!RND) {
