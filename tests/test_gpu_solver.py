@@ -159,3 +159,20 @@ def test_auto_temperature_range_on_wishart():
     assert np.isclose(min(res[0]["temps"]), lo, rtol=1e-6)
     assert np.isclose(max(res[0]["temps"]), hi, rtol=1e-6)
     assert min(2 * r["best_energy"] for r in res) == g["ground_energy_x2"]
+
+
+def test_sharded_update_single_process_equals_plain_call():
+    """Without a process group the sharded call is the plain call (rank 0,
+    seed + 0)."""
+    from pysa_gb300 import Solver
+    from pysa_gb300.shard import metropolis_update_sharded
+    rng = np.random.default_rng(2)
+    J = np.triu(rng.normal(size=(40, 40)), 1)
+    s = Solver(J + J.T, "ising", "float32")
+    kw = dict(num_sweeps=10, num_replicas=4, min_temp=0.5, max_temp=2.0)
+    a = metropolis_update_sharded(s, 5, seed=9, **kw)
+    b = s.metropolis_update(num_reads=5, seed=9, return_dataframe=False, **kw)
+    assert len(a) == 5
+    for ra, rb in zip(a, b):
+        assert (ra["states"] == rb["states"]).all()
+        assert ra["best_energy"] == rb["best_energy"]
