@@ -170,7 +170,9 @@ def test_sharded_update_single_process_equals_plain_call():
     J = np.triu(rng.normal(size=(40, 40)), 1)
     s = Solver(J + J.T, "ising", "float32")
     kw = dict(num_sweeps=10, num_replicas=4, min_temp=0.5, max_temp=2.0)
+    np.random.seed(5)  # initial states come from NumPy's global stream
     a = metropolis_update_sharded(s, 5, seed=9, **kw)
+    np.random.seed(5)
     b = s.metropolis_update(num_reads=5, seed=9, return_dataframe=False, **kw)
     assert len(a) == 5
     for ra, rb in zip(a, b):
