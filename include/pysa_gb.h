@@ -53,7 +53,10 @@ enum {
   PYSA_GB_ERR_SIZE = -2,    /* size beyond what the kernels support */
   PYSA_GB_ERR_CUDA = -3,    /* a CUDA runtime call failed */
   PYSA_GB_ERR_TIMEOUT = -4, /* (status word) a bounded device wait ran out */
-  PYSA_GB_ERR_NOBETA0 = -5  /* log-omega requested without a beta = 0 slot */
+  PYSA_GB_ERR_NOBETA0 = -5, /* log-omega requested without a beta = 0 slot */
+  PYSA_GB_ERR_DRIFT = -6    /* (status word) a chain's accumulated energy left
+                               its recomputed value by more than 1e-3 of
+                               max(1, |E|), or is not finite */
 };
 
 /* Largest number of spins per instance the sweep kernels accept. */

@@ -533,6 +533,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           if (q == 0 && valid) {
             double e = 0.0;
             for (int qq = 0; qq < F; ++qq) e += epart_s[qq * CC + c];
+            // drift check: the energy the sweeps accumulated against the one
+            // just rebuilt from the spins (not at sweep 0, whose energies
+            // may be the caller's own)
+            const double acc_e = e0_s[c] + dE_s[c];
+            if (sweep > 0 && !(fabs(acc_e - e) <= 1e-3 * fmax(1.0, fabs(e))))
+              set_status(status, PYSA_GB_ERR_DRIFT);
             e0_s[c] = (double)(float)e;
             dE_s[c] = 0.0;
           }

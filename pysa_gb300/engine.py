@@ -581,8 +581,11 @@ class PTBatch:
     def check_status(self):
         code = int(self.status.item())
         if code != 0:
-            raise _lib.LibraryError(
-                f"device reported status {code} (a bounded wait ran out)")
+            what = {-4: "a bounded wait ran out",
+                    -6: "energy drift: the accumulated energies left their "
+                        "recomputed values (non-finite or badly scaled "
+                        "couplings)"}.get(code, "device error")
+            raise _lib.LibraryError(f"device reported status {code} ({what})")
 
     # --------------------------------------------------------- read back
     def fetch(self) -> dict:

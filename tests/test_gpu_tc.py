@@ -251,3 +251,24 @@ def test_tc_random_order_mixed_batch_matches_plain():
     for k in ("spins", "energies", "beta_idx", "best_energy", "best_sweep",
               "best_spins"):
         assert (out["auto"][k] == out["plain"][k]).all(), k
+
+
+def test_energy_drift_is_reported_not_hidden():
+    """A non-finite coupling makes the in-kernel recompute disagree with the
+    accumulated energies: the status word says so and the host raises (no
+    fault, no hang: NaN arithmetic only)."""
+    from pysa_gb300 import Instance, PTBatch, pack_spins
+    from pysa_gb300._lib import LibraryError
+    rng = np.random.default_rng(4)
+    n, R, Rd = 128, 4, 2
+    J = np.triu(rng.normal(size=(n, n)), 1)
+    J = (J + J.T).astype(np.float32)
+    J[3, 7] = J[7, 3] = np.nan
+    b = PTBatch("ising", [Instance(J, np.zeros(n, np.float32),
+                                   np.ones(R, np.float32), Rd)], kernel="tc")
+    x0 = (2 * rng.integers(0, 2, (Rd, R, n)) - 1).astype(np.float32)
+    b.set_states(pack_spins(x0, "ising", b.words),
+                 np.zeros(Rd * R, np.float32))
+    b.run(8, seed=1, recompute_every=4)
+    with pytest.raises(LibraryError, match="drift"):
+        b.fetch()
