@@ -119,6 +119,12 @@ typedef struct {
   int64_t *sweep_counter; /* [1] index of the next sweep */
   int32_t *status;        /* [1] 0 or a PYSA_GB_ERR_* code from the device */
   uint32_t *ticket;       /* [1] zero-initialised scratch word */
+  uint32_t *stream_key;   /* [num_chains] or NULL: per-chain change of the
+                             sweep stream's key (0 = the plain stream);
+                             pysa_gb_propose advances a chain's entry on every
+                             proposal it accepts, so its later sweeps draw
+                             fresh uniforms instead of replaying the ones
+                             that would undo the move */
 } pysa_gb_state;
 
 /* Per-call workspace, caller-allocated (sizes from pysa_gb_workspace_bytes). */

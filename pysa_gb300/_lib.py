@@ -35,7 +35,7 @@ class State(ctypes.Structure):
     _fields_ = [("spins", P), ("energies", P), ("beta_idx", P),
                 ("chain_beta", P), ("best_energy", P), ("best_sweep", P),
                 ("best_spins", P), ("log_omega", P), ("sweep_counter", P),
-                ("status", P), ("ticket", P)]
+                ("status", P), ("ticket", P), ("stream_key", P)]
 
 
 class Workspace(ctypes.Structure):

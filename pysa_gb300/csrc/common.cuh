@@ -51,6 +51,16 @@ __device__ __forceinline__ void draw4(uint64_t seed, uint32_t tag,
                 (uint32_t)(seed >> 32), out);
 }
 
+// Key of chain `chain`'s sweep stream: the seed, changed by the chain's
+// stream key when one is set (see pysa_gb_state.stream_key).
+__device__ __forceinline__ uint64_t chain_seed(uint64_t seed,
+                                               const uint32_t* key,
+                                               int64_t chain) {
+  if (!key) return seed;
+  const uint32_t k = key[chain];
+  return k ? seed ^ ((uint64_t)k * 0x9E3779B97F4A7C15ull) : seed;
+}
+
 __device__ __forceinline__ uint32_t draw1(uint64_t seed, uint32_t tag,
                                           uint32_t inst, uint32_t a,
                                           uint32_t b, uint32_t idx) {

@@ -268,6 +268,7 @@ __global__ void k_mh_accept(const pysa_gb_problems p, pysa_gb_state s,
   }
   if (lane == 0) {
     s.energies[c] = e_new;
+    if (s.stream_key) s.stream_key[c] += 1u;  // fresh sweep stream
     if (improved) {
       s.best_energy[c] = e_new;
       const int64_t sw = *s.sweep_counter;

@@ -138,6 +138,8 @@ __global__ void __launch_bounds__(kCsrChains) k_sweep_csr(const CsrArgs a) {
 
   const float beta = valid ? a.s.chain_beta[chain] : 0.0f;
   const uint32_t cl = (uint32_t)(chain - a.p.chain_off[inst]);
+  const uint64_t seed_c =
+      valid ? chain_seed(a.seed, a.s.stream_key, chain) : a.seed;
   const int32_t* rows =
       D > 0 ? nullptr : a.p.csr_rows + a.p.csr_row_off[inst] * 9;
   const int32_t* colp = a.p.csr_col + a.p.csr_ent_off[inst];
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(kCsrChains) k_sweep_csr(const CsrArgs a) {
     if (b + 1 < nb) stage(b + 1);
     for (int t0 = 32 * b; t0 < n && t0 < 32 * b + 32; t0 += 4) {
       uint32_t rnd[4];
-      draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, cl,
+      draw4(seed_c, TAG_SWEEP, (uint32_t)inst, sweep, cl,
             (uint32_t)(t0 >> 2), rnd);
       // short records: all four up front, ahead of the flips' shared
       // stores; long ones one at a time (registers)

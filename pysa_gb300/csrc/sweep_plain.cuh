@@ -195,7 +195,10 @@ __global__ void __launch_bounds__(W * 32, 1)
           const int P = j * 32 + lane, g = P >> 3, q = P & 7;
           const int gg = g < GW ? g : 0;
           const uint32_t cl = (uint32_t)(item.chain0 + g0 + gg - chain_base);
-          draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, cl,
+          draw4(g0 + gg < item.nchains
+                    ? chain_seed(a.seed, a.s.stream_key, item.chain0 + g0 + gg)
+                    : a.seed,
+                TAG_SWEEP, (uint32_t)inst, sweep, cl,
                 (uint32_t)((t >> 2) + q), rnd[j]);
         }
         if (!RANDOM) {

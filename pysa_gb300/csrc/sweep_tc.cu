@@ -813,7 +813,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 rx.valid = valid;
                 rx.ising = ising;
                 rx.beta = beta;
-                rx.seed = a.seed;
+                rx.seed = chain_seed(a.seed, a.s.stream_key, chain);
                 rx.inst = (uint32_t)inst;
                 rx.sweep = sweep;
                 rx.chain_local = chain_local;
@@ -1260,8 +1260,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             for (int it = hid; it < CC * 16; it += 64) {
               const int c2 = it % CC, quad = it / CC;
               const uint32_t cl = (uint32_t)(item.chain0 + c2 - chain_base);
+              const uint64_t sk =
+                  c2 < item.nchains
+                      ? chain_seed(a.seed, a.s.stream_key, item.chain0 + c2)
+                      : a.seed;
               uint32_t x[4];
-              draw4(a.seed, TAG_SWEEP, (uint32_t)inst, sweep, cl,
+              draw4(sk, TAG_SWEEP, (uint32_t)inst, sweep, cl,
                     (uint32_t)(16 * t + quad), x);
 #pragma unroll
               for (int e = 0; e < 4; ++e)

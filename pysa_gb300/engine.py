@@ -415,6 +415,16 @@ class PTBatch:
         self.autotune_ms = times
         return times
 
+    def enable_stream_keys(self):
+        """Per-chain sweep-stream keys (all 0: the plain streams); accepted
+        proposals (pysa_gb_propose) advance their chain's key so its later
+        sweeps draw fresh uniforms.  Done once per batch."""
+        if getattr(self, "stream_key", None) is None:
+            self.stream_key = torch.zeros(max(self.num_chains, 1),
+                                          dtype=torch.int32,
+                                          device=self.device)
+            self.s.stream_key = _ptr(self.stream_key)
+
     # ---------------------------------------------- device-resident inputs
     def load_problem(self, inst: int, P: torch.Tensor):
         """Couplings and fields of instance `inst` from a dense symmetric

@@ -257,6 +257,10 @@ def run_with_proposals(batch: PTBatch, prop: LearnedProposal | None,
     if prop is None:
         batch.run(num_sweeps, seed=seed, use_pt=use_pt)
         return None
+    # a chain that accepts a proposal continues on a fresh sweep stream;
+    # on the shared counter-based stream its next sweeps would replay the
+    # uniforms of the unmoved chain and largely undo the move
+    batch.enable_stream_keys()
     interval = max(int(interval), 1)
     train_every = interval if train_every is None else max(int(train_every), 1)
     step = math.gcd(interval, train_every)
