@@ -278,10 +278,16 @@ def run_tts_workload(args, w, rank, world):
             torch.cuda.synchronize()
             arms["learned"][S] = (time.perf_counter() - t0, per_read_best(b))
             b.check_status()
+            pb = arms["plain"][S][1]
+            lb = arms["learned"][S][1]
             stats[S] = {"rounds": st.rounds, "train_steps": st.train_steps,
                         "acceptance_mean": float(st.acceptance.mean()),
                         "accepted_moves": int(st.accepted.sum()),
-                        "enabled_instances_at_end": int(st.enabled.sum())}
+                        "enabled_instances_at_end": int(st.enabled.sum()),
+                        "chains_moved_to_new_streams":
+                            int((b.stream_key != 0).sum().item()),
+                        "reads_best_lower_than_plain": int((lb < pb).sum()),
+                        "reads_best_higher_than_plain": int((lb > pb).sum())}
             del b, prop
     for arm in arms.values():
         for S, (_, best) in arm.items():
