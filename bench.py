@@ -1047,8 +1047,11 @@ def main():
         rows = solver.metropolis_update(**kw, seed=2)
         e2e_s = time.perf_counter() - t0
         words = batch.words
-        h2d = 4 * n * n + 4 * n + 4 * R + C * words * 4 + C * 4
-        d2h = C * (words * 4 * 2 + 4 * 4)
+        # couplings, fields, ladder, float32 states (packed on the device);
+        # float32 final states, spin words of the best states, per-chain
+        # energies, slots, best energies and sweeps
+        h2d = 4 * n * n + 4 * n + 4 * R + C * n * 4
+        d2h = C * (n * 4 + words * 4 * 2 + 4 * 4)
         e2e = {"value": Rd * R * n * sweeps_e2e / e2e_s, "unit": "attempts/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "sweeps_per_call": sweeps_e2e, "seconds": e2e_s,

@@ -303,8 +303,17 @@ class Solver(object):
         words = batch.words
         e0 = None if energies_given is None else np.tile(
             np.asarray(energies_given, np.float32), Rd)
-        batch.set_states(pack_spins(states0, self.problem_type, words), e0,
-                         best_global=not parallel)
+        if Rd:
+            # the states travel as float32 and are packed on the device
+            import torch
+            batch.set_states_device(
+                torch.from_numpy(np.ascontiguousarray(
+                    states0.reshape(Rd * R, N), dtype=np.float32)),
+                None if e0 is None else torch.from_numpy(e0),
+                best_global=not parallel)
+        else:
+            batch.set_states(pack_spins(states0, self.problem_type, words),
+                             e0, best_global=not parallel)
         init_e = None
         if not parallel:
             import torch
@@ -313,14 +322,18 @@ class Solver(object):
         t1 = time()
         batch.run(int(num_sweeps), seed=int(seed), update=update_strategy,
                   use_pt=bool(use_pt), log_omega=bool(get_part_fun))
+        # final states unpacked on the device, copied as float32
+        states_dev = batch.unpack_device() if Rd else None
         res = batch.fetch()
         t2 = time()
         init_us = int((t1 - t0) * 1e6 / max(Rd, 1))
         run_us = int((t2 - t1) * 1e6 / max(Rd, 1))
 
-        spins = res['spins'].reshape(Rd, R, words)
-        out_states_all = unpack_spins(spins, N, self.problem_type,
-                                      self.float_type)
+        if Rd:
+            out_states_all = states_dev.cpu().numpy().reshape(Rd, R, N).astype(
+                self.float_type, copy=False)
+        else:
+            out_states_all = np.zeros((0, R, N), self.float_type)
         energies = res['energies'].reshape(Rd, R).astype(self.float_type)
         bidx = res['beta_idx'].reshape(Rd, R).astype(np.int64)
         be = res['best_energy'].reshape(Rd, R)
