@@ -392,7 +392,7 @@ def run_batch_workload(args, w, rank, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
     value = attempts * args.steps * world / total_s
-    # graph-captured chunk of 64 sweeps (the production path), one timing
+    # graph-captured chunks (the production path), one timing
     g0 = time.perf_counter()
     batch.run(128, seed=3, graph_chunk=64)
     torch.cuda.synchronize()
@@ -908,11 +908,11 @@ def main():
                         device="cuda")
     # With every instance on the tensor cores and R dividing the chains per
     # CTA, a launch runs several sweeps with the exchange fused in and the
-    # fields resident in tensor memory: time launches of 64 sweeps (the
+    # fields resident in tensor memory: time launches of 128 sweeps (the
     # library's launch size; L2 flushed before each).  Otherwise time each
     # sweep and its exchange.
     fused = bool(use_tc and batch.ws.plain_live == 0 and batch.ws.tc_fusable)
-    chunk = 64 if fused else 1
+    chunk = 128 if fused else 1
     iters = []
     done = 0
     while done < args.steps:
@@ -1099,7 +1099,12 @@ def main():
             "clocks": sampler.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
-            "gpu_launches": (len(iters) if fused else
+            # fused: one persistent launch per chunk of up to 128 sweeps, or
+            # in random order per group of tc_rand_slots sweeps a visiting-
+            # order kernel, a repack kernel and the sweep launch
+            "gpu_launches": ((sum(3 * -(-c // int(batch.ws.tc_rand_slots))
+                                  for c in iters) if upd else len(iters))
+                             if fused else
                              2 * args.steps + (args.steps if upd else 0)),
         }
         print(json.dumps(line), flush=True)

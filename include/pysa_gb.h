@@ -164,7 +164,7 @@ typedef struct {
   int32_t *tc_sched;        /* [2 + tc_num_items] device scratch of the
                                persistent tensor-core kernel */
   int32_t tc_unit_sweeps;   /* sweeps per work unit of that kernel (0: 8) */
-  int32_t tc_launch_sweeps; /* most sweeps one launch of it covers (0: 64) */
+  int32_t tc_launch_sweeps; /* most sweeps one launch of it covers (0: 128) */
   /* random visiting order on the tensor cores: J tiles and diagonal blocks
    * repacked in each sweep's order, tc_rand_slots sweeps at a time (0: random
    * sweeps run on the plain kernel); needs perm_slots >= tc_rand_slots */
@@ -222,7 +222,7 @@ int pysa_gb_abi_version(void);
 const char *pysa_gb_last_error(void);
 
 /* Diagnostics: when `device_buffer` (>= 24 x 64 uint64) is not NULL, the
- * tensor-core sweep records a per-block globaltimer timeline of its first CTA
+ * tensor-core sweep records a per-block timeline (SM clock cycles) of its first CTA
  * there: [0] decision start, [1] fields ready, [2] decisions done, [3] A free,
  * [4] A published, [5] MMA start, [6] next-block fields committed, [7] stages
  * issued, [8 + 3g .. 10 + 3g] sub-block g: fields loaded, lazy corrections

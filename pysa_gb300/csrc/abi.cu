@@ -66,7 +66,7 @@ static int cuda_fail(cudaError_t e, const char* where) {
 }
 
 // Default for the most sweeps one fused tensor-core launch covers.
-constexpr int kMaxFusedSweeps = 64;
+constexpr int kMaxFusedSweeps = 128;
 
 // Streaming multiprocessors of the current device (cached per device).
 static inline bool is_sparse(const pysa_gb_host_tables* h, int i) {

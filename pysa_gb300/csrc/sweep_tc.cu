@@ -98,7 +98,8 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
   }
 }
 
-// Timeline stamps of CTA 0 when a trace buffer is given, in builds with
+// Timeline stamps (SM clock cycles) of CTA 0 when a trace buffer is given,
+// in builds with
 // PYSA_GB_TRACE defined (diagnostics only: the stamps' branches in the
 // decision loop cost about 8 % of a sweep, so release builds drop them):
 // row G < 48 per block, row 48 whole-unit marks (entry, set-up done, last
@@ -106,12 +107,12 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
 __device__ __forceinline__ void stamp(const TcArgs& a, uint32_t G, int slot) {
 #ifdef PYSA_GB_TRACE
   if (a.trace && blockIdx.x == 0 && G < 48)
-    a.trace[G * 24 + slot] = globaltimer_ns();
+    a.trace[G * 24 + slot] = clock64();
 #endif
 }
 __device__ __forceinline__ void stamp_cta(const TcArgs& a, int slot) {
 #ifdef PYSA_GB_TRACE
-  if (a.trace && blockIdx.x == 0) a.trace[48 * 24 + slot] = globaltimer_ns();
+  if (a.trace && blockIdx.x == 0) a.trace[48 * 24 + slot] = clock64();
 #endif
 }
 

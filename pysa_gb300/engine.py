@@ -530,7 +530,7 @@ class PTBatch:
     # ------------------------------------------------------------ sweeps
     def run(self, num_sweeps: int, *, seed: int, update: str = "sequential",
             use_pt: bool = True, log_omega: bool = False,
-            graph_chunk: int = 64, recompute_every: int | None = None,
+            graph_chunk: int = 128, recompute_every: int | None = None,
             final_recompute: bool = True):
         """Sweeps with exchange.  recompute_every: the tensor-core path
         rebuilds fields and energies from the spins every that many sweeps
