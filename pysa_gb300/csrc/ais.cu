@@ -161,6 +161,100 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
   }
 }
 
+// Small instances (n <= 32): one thread per sample, its spins in one word
+// and its fields in a shared-memory column [32][128] (conflict-free), the
+// instance's couplings in shared memory too (the row of the visited spin is
+// the same for every thread: a broadcast).  The arithmetic is k_ais's: the
+// same f32 field updates (a rejected attempt adds 0 * J, which changes no
+// field but possibly the sign of a zero), the same f64 energy and weights,
+// the same uniforms (one draw of 4 per 4 steps instead of one per step).
+// No shuffles or ballots, and a warp covers 32 samples instead of 8.
+__global__ void __launch_bounds__(128) k_ais_small(const AisArgs a) {
+  __shared__ float Js[32 * 32];
+  __shared__ float Hs[32 * 128];
+  const int inst = blockIdx.y;
+  const int tid = threadIdx.x;
+  if (a.replicas[inst] != 1) {
+    if (blockIdx.x == 0 && tid == 0) set_status(a.status, PYSA_GB_ERR_ARG);
+    return;
+  }
+  const int n = a.n_tab[inst];
+  const int ld = a.ld_tab[inst];
+  const int64_t samples = a.reads[inst];
+  if ((int64_t)blockIdx.x * blockDim.x >= samples) return;  // whole CTA
+  const float* Jp = a.J + a.j_off[inst];
+  for (int e = tid; e < 32 * 32; e += blockDim.x) {
+    const int r = e >> 5, c = e & 31;
+    Js[e] = (r < n && c < n) ? Jp[(int64_t)r * ld + c] : 0.0f;
+  }
+  const int64_t my = (int64_t)blockIdx.x * blockDim.x + tid;
+  const bool valid = my < samples;
+  const int64_t myc = a.chain_off[inst] + (valid ? my : 0);
+  float* H = Hs + tid;  // field of spin c at H[c * 128]
+  for (int c = 0; c < 32; ++c)
+    H[c * 128] = (valid && c < n) ? a.fields[myc * a.field_ld + c] : 0.0f;
+  __syncthreads();
+  if (!valid) return;
+  const bool ising = a.problem_type == PYSA_GB_ISING;
+  uint32_t word = a.spins[myc * a.words];
+  double E = (double)a.energies[myc];
+  int ones = __popc(word);
+  double lw = 0.0;
+  float beta_old = 0.0f;
+  const double lr = a.ref == 1 ? log((1.0 - a.p) / a.p) : 0.0;
+  const double logp = a.ref == 1 ? log(a.p) : 0.0;
+  const double log1p_ = a.ref == 1 ? log(1.0 - a.p) : 0.0;
+  for (int k = 0; k < a.num_temps; ++k) {
+    const float beta = a.temps[k];
+    if (a.order == 1) {
+      const float e = (float)E;
+      const double re = -((double)(n - ones) * logp + (double)ones * log1p_);
+      lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
+            ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+    }
+    const int32_t* perm =
+        a.perm + ((int64_t)k * a.num_instances + inst) * a.max_n;
+    uint32_t rnd[4];
+    for (int t = 0; t < n; ++t) {
+      if ((t & 3) == 0)
+        draw4(a.seed, TAG_AIS, (uint32_t)inst, (uint32_t)k, (uint32_t)my,
+              (uint32_t)(t >> 2), rnd);
+      const uint32_t x = (t & 3) == 0 ? rnd[0] : (t & 3) == 1 ? rnd[1]
+                         : (t & 3) == 2 ? rnd[2] : rnd[3];
+      const int i = a.update == PYSA_GB_RANDOM ? perm[t] : t;
+      const float hv = H[i * 128];
+      const bool sbit = (word >> i) & 1u;
+      const float dn = ising ? (sbit ? 2.0f * hv : -2.0f * hv)
+                             : (sbit ? hv : -hv);
+      const double refd = sbit ? -lr : lr;  // bit going down : up
+      const double full =
+          (double)beta * (double)dn + (1.0 - (double)beta) * refd;
+      const bool acc = accept_full(full, x);
+      if (acc) {
+        E -= (double)dn;
+        ones += sbit ? -1 : 1;
+        word ^= 1u << i;
+      }
+      const float d = acc ? (ising ? (sbit ? -2.0f : 2.0f)
+                                   : (sbit ? -1.0f : 1.0f))
+                          : 0.0f;
+      const float* Jr = Js + i * 32;
+#pragma unroll 8
+      for (int c = 0; c < n; ++c) H[c * 128] = fmaf(d, Jr[c], H[c * 128]);
+    }
+    if (a.order == 0) {
+      const float e = (float)E;
+      const double re = -((double)(n - ones) * logp + (double)ones * log1p_);
+      lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
+            ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+    }
+    beta_old = beta;
+  }
+  a.log_w[myc] = lw;
+  a.energies[myc] = (float)E;
+  a.spins[myc * a.words] = word;
+}
+
 // Warp per sample keeps the code simple for the small n AIS is used on;
 // GW samples per warp amortise the decision shuffles.
 template <int NC, int GW>
@@ -174,6 +268,12 @@ static cudaError_t launch_ais_t(const AisArgs& a, int64_t max_samples,
 }
 
 cudaError_t launch_ais(const AisArgs& a, int64_t max_samples, cudaStream_t st) {
+  if (a.max_n <= 32) {
+    const int64_t blocks = (max_samples + 127) / 128;
+    dim3 grid((unsigned)(blocks > 0 ? blocks : 1), (unsigned)a.num_instances);
+    k_ais_small<<<grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
+  }
   const int nc = (a.max_n + 31) / 32;
   if (nc <= 1) return launch_ais_t<1, 8>(a, max_samples, st);
   if (nc <= 2) return launch_ais_t<2, 8>(a, max_samples, st);
