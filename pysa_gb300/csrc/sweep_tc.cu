@@ -650,9 +650,14 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             // error of __logf plus the two roundings of a threshold); in
             // between, the exact f64 rule decides.  With beta <= 0 every
             // flip is accepted (log u < 0 <= beta * dn).
+            // Lanes without a chain decide too (their rows of A only touch
+            // their own TMEM lanes and their state is never written back):
+            // with a zero band (th == tl) they never ask for the exact rule.
+            // beta <= 0 makes 1 / beta infinite: th = -inf accepts all.
             const float scale = ising ? 2.0f : 1.0f;
-            const bool bpos = beta > 0.0f;
-            const float invbs = bpos ? 1.0f / (beta * scale) : 0.0f;
+            const float invbs = beta > 0.0f ? 1.0f / (beta * scale) : INFINITY;
+            const float band0 = valid ? 3e-5f : 0.0f;
+            const float band1 = valid ? 1e-6f : 0.0f;
             // the previous sub-block's deltas (its corrections of this one
             // and its A rows come from registers)
             float dprev[16];
@@ -750,6 +755,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               uint32_t wcur = g < 2 ? w0 : w1;
               const int sb = 16 * (g & 1);
               const uint32_t sbits = wcur >> sb;  // spins before the sub-block
+              // bit j: position 16 g + j of the block exists (< kmax)
+              const int nlive = kmax - 16 * g;
+              const uint32_t live_mask =
+                  nlive >= 16 ? 0xFFFFu : nlive > 0 ? (1u << nlive) - 1u : 0u;
               float lfv[16];
 #pragma unroll
               for (int j = 0; j < 16; ++j) lfv[j] = lfb[(16 * g + j) * CC + c];
@@ -766,17 +775,15 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               for (int j = 0; j < 16; ++j) {
                 const int k = 16 * g + j;
                 const float lfk = lfv[j];
-                const float m = fmaf(1e-6f, fabsf(lfk), 3e-5f);
-                const bool live = valid && k < kmax;
-                const float th =
-                    !live ? INFINITY
-                          : bpos ? fminf((lfk + m) * invbs, 0.0f) : -INFINITY;
-                const float tl =
-                    !live ? INFINITY : bpos ? (lfk - m) * invbs : -INFINITY;
+                const float m = fmaf(band1, fabsf(lfk), band0);
+                const float th = fminf((lfk + m) * invbs, 0.0f);
+                const float tl = (lfk - m) * invbs;
                 const bool sbit = (sbits >> j) & 1u;
                 const float x = sbit ? hs[j] : -hs[j];
-                const bool acc = x >= th;
-                unc |= !acc && !(x < tl);
+                const bool sure = x >= th;
+                // positions past n (zero fields: x = 0 >= th) never flip
+                const bool acc = sure && ((live_mask >> j) & 1u);
+                unc |= !sure && !(x < tl);
                 const float dl = acc ? (sbit ? -scale : scale) : 0.0f;
                 dcur[j] = dl;
                 dEb = acc ? fmaf(-scale, x, dEb) : dEb;
