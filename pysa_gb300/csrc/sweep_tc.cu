@@ -770,6 +770,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               const uint32_t wsave = wcur;
               const float dEsave = dEb;
               bool unc = false;
+              uint32_t flips = 0u;  // bit j: spin 16 g + j flipped
               float dcur[16];
     #pragma unroll
               for (int j = 0; j < 16; ++j) {
@@ -786,8 +787,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 unc |= !sure && !(x < tl);
                 const float dl = acc ? (sbit ? -scale : scale) : 0.0f;
                 dcur[j] = dl;
-                dEb = acc ? fmaf(-scale, x, dEb) : dEb;
-                wcur ^= acc ? (1u << (sb + j)) : 0u;
+                dEb = fmaf(dl, hs[j], dEb);  // dl h = -dn exactly; 0 if kept
+                flips |= acc ? (1u << j) : 0u;
                 if (j < 15) {  // exact corrections inside the sub-block
                   const float4* jr =
                       reinterpret_cast<const float4*>(jb + k * 64 + 16 * g);
@@ -801,6 +802,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   }
                 }
               }
+              wcur ^= flips << sb;
               if (__any_sync(0xffffffffu, unc)) {
                 // rare: the whole sub-block again with the exact f64 rule
                 // where needed (out of line)
