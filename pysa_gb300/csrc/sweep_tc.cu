@@ -656,8 +656,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             // beta <= 0 makes 1 / beta infinite: th = -inf accepts all.
             const float scale = ising ? 2.0f : 1.0f;
             const float invbs = beta > 0.0f ? 1.0f / (beta * scale) : INFINITY;
-            const float band0 = valid ? 3e-5f : 0.0f;
-            const float band1 = valid ? 1e-6f : 0.0f;
+            // the band in field units: (3e-5 + 1e-6 |log u|) / (beta scale);
+            // none at beta = 0 (t = -inf: every move accepted)
+            const bool banded = valid && invbs < INFINITY;
+            const float band0 = banded ? 3e-5f * invbs : 0.0f;
+            const float band1 = banded ? 1e-6f * invbs : 0.0f;
             // the previous sub-block's deltas (its corrections of this one
             // and its A rows come from registers)
             float dprev[16];
@@ -776,15 +779,17 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               for (int j = 0; j < 16; ++j) {
                 const int k = 16 * g + j;
                 const float lfk = lfv[j];
+                const float t = lfk * invbs;
                 const float m = fmaf(band1, fabsf(lfk), band0);
-                const float th = fminf((lfk + m) * invbs, 0.0f);
-                const float tl = (lfk - m) * invbs;
+                const float th = fminf(t + m, 0.0f);
+                const float tl = t - m;
                 const bool sbit = (sbits >> j) & 1u;
                 const float x = sbit ? hs[j] : -hs[j];
-                const bool sure = x >= th;
-                // positions past n (zero fields: x = 0 >= th) never flip
-                const bool acc = sure && ((live_mask >> j) & 1u);
-                unc |= !sure && !(x < tl);
+                // positions past n have zero fields (x = 0 >= th): their
+                // "flips" change no field and no energy and are masked out
+                // of the spin word below
+                const bool acc = x >= th;
+                unc |= !acc && !(x < tl);
                 const float dl = acc ? (sbit ? -scale : scale) : 0.0f;
                 dcur[j] = dl;
                 dEb = fmaf(dl, hs[j], dEb);  // dl h = -dn exactly; 0 if kept
@@ -802,7 +807,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   }
                 }
               }
-              wcur ^= flips << sb;
+              wcur ^= (flips & live_mask) << sb;
               if (__any_sync(0xffffffffu, unc)) {
                 // rare: the whole sub-block again with the exact f64 rule
                 // where needed (out of line)
