@@ -626,6 +626,23 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           go = __all_sync(0xffffffffu, go);
           const bool lead = go && c == 0;
           if (lead) stamp(a, Gb, 0);
+          // one sub-block's deltas of chain c into its A rows of every slice
+          auto put_a = [&](int gg, const float* d) {
+            uint32_t pkg[8];
+#pragma unroll
+            for (int j = 0; j < 16; j += 2)
+              pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
+#pragma unroll
+            for (int qq = 0; qq < F; ++qq) {
+              const int m = qq * CC + c;
+              unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+                                    ((m >> 3) * 8) * 128 + (m & 7) * 16;
+              *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
+                  make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+              *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
+                  make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
+            }
+          };
           if (go) {
             tc::fence_after_sync();
             if (lead) stamp(a, Gb, 1);
@@ -667,23 +684,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) dprev[j] = 0.0f;
             bool a_early = false;
-            // one sub-block's deltas into the A rows of every slice
-            auto put_a = [&](int gg, const float* d) {
-              uint32_t pkg[8];
-#pragma unroll
-              for (int j = 0; j < 16; j += 2)
-                pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
-#pragma unroll
-              for (int qq = 0; qq < F; ++qq) {
-                const int m = qq * CC + c;
-                unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                      ((m >> 3) * 8) * 128 + (m & 7) * 16;
-                *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
-                    make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
-                *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
-                    make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
-              }
-            };
             // fields of sub-block g with the corrections of every earlier
             // sub-block of the block
             auto fields = [&](int g, float* hs) {
@@ -845,18 +845,27 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               // block's MMAs must be done first.  After the second sub-block
               // they usually are (one slice's worth of MMAs); if not (long
               // MMAs at fold 4), the rows wait for the block's end
-              if (g == 1)
-                a_early = Gb == G0 || mbar_test_wait(sh.mma_done, (Gb - 1) & 1);
-              if (a_early && g >= 1) {
-                if (g == 1) put_a(0, dprev);
-                put_a(g, dcur);
+              if constexpr (C::HELP) {
+                // the helpers write the rows of sub-blocks 0 to 2; the last
+                // sub-block's here (the previous block's MMAs are long done)
+                if (g == 3 && (Gb == G0 || tc_wait(sh.mma_done, (Gb - 1) & 1,
+                                                   sh, status)))
+                  put_a(3, dcur);
+              } else {
+                if (g == 1)
+                  a_early =
+                      Gb == G0 || mbar_test_wait(sh.mma_done, (Gb - 1) & 1);
+                if (a_early && g >= 1) {
+                  if (g == 1) put_a(0, dprev);
+                  put_a(g, dcur);
+                }
               }
 #pragma unroll
               for (int j = 0; j < 16; ++j) dprev[j] = dcur[j];
               if (lead) stamp(a, Gb, 10 + 3 * g);
               if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
             }
-            if (!a_early) {
+            if (!C::HELP && !a_early) {
               if (Gb > G0) {
                 if (lead) stamp(a, Gb, 2);
                 const bool a_ok =
@@ -932,6 +941,26 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     #pragma unroll
               for (int j = 0; j < 16; ++j) corr_s[j * CC + c] = c2[j];
             }
+            // A rows of the decided sub-blocks below `upto`, once the
+            // previous block's MMAs are done with A (tested without waiting
+            // until the last call, so the deciders never wait for it here)
+            int na = 0;
+            auto put_decided = [&](int upto, bool block) {
+              if (!hgo || na >= upto) return;
+              bool ready =
+                  Gb == G0 || mbar_test_wait(sh.mma_done, (Gb - 1) & 1);
+              if (!ready && block)
+                ready = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
+              if (!ready) return;
+              for (; na < upto; ++na) {
+                float d[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                  d[j] = dl_s[(16 * na + j) * CC + c];
+                put_a(na, d);
+              }
+            };
+            put_decided(1, false);
             named_sync_dec();  // sub-block 1 decided; corrections of 2 out
             if (hok) {
     #pragma unroll 2
@@ -950,7 +979,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     #pragma unroll
               for (int j = 0; j < 16; ++j) corr_s[(16 + j) * CC + c] = c3[j];
             }
+            put_decided(2, false);
             named_sync_dec();  // sub-block 2 decided; corrections of 3 out
+            put_decided(3, true);
+            fence_proxy_async();
           }
           if (lane == 0) stamp(a, Gb, 20 + warp);
           named_sync_128();
@@ -1084,12 +1116,14 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           const uint32_t b0 = smem_base +
                               (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
                               (uint32_t)(r_lo / 8) * 1024u;
+          // K steps of 16 are 256 bytes apart: 16 in the descriptors'
+          // address field (shared addresses stay below 2^18)
+          const uint64_t ad = tc::smem_desc(a0, 128, 1024);
+          const uint64_t bd = tc::smem_desc(b0, 128, 1024);
 #pragma unroll
           for (int ks = 0; ks < 4; ++ks)
-            tc::mma_bf16(taddr + 256 * j + r_lo,
-                         tc::smem_desc(a0 + 256 * ks, 128, 1024),
-                         tc::smem_desc(b0 + 256 * ks, 128, 1024), idesc,
-                         (acc | (uint32_t)ks) ? 1u : 0u);
+            tc::mma_bf16(taddr + 256 * j + r_lo, ad + 16u * ks, bd + 16u * ks,
+                         idesc, (acc | (uint32_t)ks) ? 1u : 0u);
         };
         bool ok = true;
         for (int s = 0; s < KU && ok; ++s) {
@@ -1124,18 +1158,20 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           }
           for (int t = 0; t < NB && ok; ++t) {
             const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
+            // the next block's 64 columns (next sweep's first block after the
+            // last): slice qn, tile jf, rows r0 .. r0+63.  Worked out before
+            // the wait: the deciders wait for the MMAs that use them
+            const bool has_next = Gb + 1 < Gend;
+            const int tn = t + 1 < NB ? t + 1 : 0;
+            const int qn = (64 * tn) / S, cn = 64 * tn - qn * S;
+            const int jf = has_next ? cn >> 8 : 0, r0 = cn & 255;
+            asm volatile("" ::"r"(jf), "r"(r0), "r"(qn));
             if (!tc_wait(sh.a_full, Gb & 1, sh, status)) {
               ok = false;
               break;
             }
             stamp(a, Gb, 5);
             tc::fence_after_sync();
-            // the next block's 64 columns (next sweep's first block after the
-            // last): slice qn, tile jf, rows r0 .. r0+63
-            const bool has_next = Gb + 1 < Gend;
-            const int tn = (t + 1) % NB;
-            const int cn = (64 * tn) % S, qn = (64 * tn) / S;
-            const int jf = has_next ? cn / 256 : 0, r0 = cn % 256;
             for (int jj = 0; jj < NT && ok; ++jj) {
               const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
               const int width = S - 256 * j < 256 ? S - 256 * j : 256;
