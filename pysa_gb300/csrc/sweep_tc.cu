@@ -98,6 +98,13 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
   }
 }
 
+// (sum, compensation) + x with Neumaier's compensated summation in f32
+__device__ __forceinline__ float2 add_compensated(float2 acc, float x) {
+  const float t = acc.x + x;
+  const float e = fabsf(acc.x) >= fabsf(x) ? (acc.x - t) + x : (x - t) + acc.x;
+  return make_float2(t, acc.y + e);
+}
+
 // Timeline stamps (SM clock cycles) of CTA 0 when a trace buffer is given,
 // in builds with
 // PYSA_GB_TRACE defined (diagnostics only: the stamps' branches in the
@@ -506,7 +513,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           tc::fence_after_sync();
           // H = J s + h in TMEM; energies sum_j s_j ((J s)_j / 2 + h_j)
           const float* hh = a.p.h + a.p.h_off[inst];
-          double ep = 0.0;
+          // energy terms s_j (v_j / 2 + h_j), each split exactly into two
+          // f32 parts and summed with Neumaier's compensation: f64
+          // accuracy from the FP32 pipe
+          float2 ep = make_float2(0.0f, 0.0f);
           if (__all_sync(0xffffffffu, !*sh.abort)) {
             for (int j0 = 0; j0 < S; j0 += 32) {
               float v[32];
@@ -516,10 +526,15 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 const int col = q * S + j0 + i;
                 if (col < n) {
                   const uint32_t wv = spins_s[(col >> 5) * CC + c];
-                  const double sj =
-                      ((wv >> (col & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+                  const float sj =
+                      ((wv >> (col & 31)) & 1u) ? 1.0f : (ising ? -1.0f : 0.0f);
                   const float hj = hh[col];
-                  ep += sj * (0.5 * (double)v[i] + (double)hj);
+                  const float hv = 0.5f * v[i];  // exact
+                  const float hi = hv + hj;
+                  const float bp = hi - hv;
+                  const float lo = (hv - (hi - bp)) + (hj - bp);  // hv+hj-hi
+                  ep = add_compensated(ep, sj * hi);
+                  ep.y += sj * lo;
                   v[i] = v[i] + hj;
                 }
               }
@@ -527,7 +542,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             }
             tc::tmem_wait_st();
           }
-          epart_s[q * CC + c] = ep;
+          epart_s[q * CC + c] = (double)ep.x + (double)ep.y;
           tc::fence_before_sync();
           named_sync_128();
           tc::fence_after_sync();
