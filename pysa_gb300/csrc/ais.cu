@@ -18,6 +18,33 @@
 
 namespace pysa_gb {
 
+// accept_full on full = beta dn + (1 - beta) refd.  With the uniform
+// reference (refd = 0) full = beta dn is exact in f64 and its f32 rounding
+// is the f32 product, so the fast path runs on the FP32 pipe (far faster
+// than this GPU's FP64 one) and f64 is left to the band's exact rule; the
+// decisions are accept_full's.
+__device__ __forceinline__ bool ais_accept(float beta, float dn, bool sbit,
+                                           double lr, bool uniform_ref,
+                                           uint32_t x) {
+  if (!uniform_ref) {
+    const double refd = sbit ? -lr : lr;  // bit going down : up
+    return accept_full(
+        (double)beta * (double)dn + (1.0 - (double)beta) * refd, x);
+  }
+  if (dn != dn) return false;  // as accept_full on a NaN
+  // full >= 0: a zero factor or factors of one sign
+  if (dn == 0.0f || beta == 0.0f || ((dn > 0.0f) == (beta > 0.0f)))
+    return true;
+  const float ff = beta * dn;  // == (float)full
+  if (ff < -24.0f) return false;
+  const float uf = __uint2float_rn(x) * 0x1p-32f + 0x1p-33f;
+  const float lf = __logf(uf);
+  const float margin = 3e-5f + 1e-6f * fabsf(ff);
+  if (lf < ff - margin) return true;
+  if (lf > ff + margin) return false;
+  return accept_full_slow((double)beta * (double)dn, x);
+}
+
 template <int NC, int GW>
 __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -100,13 +127,11 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
       const bool sbit = (word >> l) & 1u;
       const float dn = ising ? (sbit ? 2.0f * hv : -2.0f * hv)
                              : (sbit ? hv : -hv);
-      const double refd = sbit ? -lr : lr;  // bit going down : up
       bool acc = false;
       if (lane_valid) {
         const uint32_t x = draw1(a.seed, TAG_AIS, (uint32_t)inst, (uint32_t)k,
                                  (uint32_t)my, (uint32_t)t);
-        const double full = (double)beta * (double)dn + (1.0 - (double)beta) * refd;
-        acc = accept_full(full, x);
+        acc = ais_accept(beta, dn, sbit, lr, a.ref != 1, x);
       }
       const uint32_t am = __ballot_sync(0xffffffffu, acc);
       const uint32_t sm = __ballot_sync(0xffffffffu, sbit);
@@ -226,10 +251,7 @@ __global__ void __launch_bounds__(128) k_ais_small(const AisArgs a) {
       const bool sbit = (word >> i) & 1u;
       const float dn = ising ? (sbit ? 2.0f * hv : -2.0f * hv)
                              : (sbit ? hv : -hv);
-      const double refd = sbit ? -lr : lr;  // bit going down : up
-      const double full =
-          (double)beta * (double)dn + (1.0 - (double)beta) * refd;
-      const bool acc = accept_full(full, x);
+      const bool acc = ais_accept(beta, dn, sbit, lr, a.ref != 1, x);
       if (acc) {
         E -= (double)dn;
         ones += sbit ? -1 : 1;
