@@ -45,6 +45,20 @@ __device__ __forceinline__ bool ais_accept(float beta, float dn, bool sbit,
   return accept_full_slow((double)beta * (double)dn, x);
 }
 
+// Log-weight increment of one temperature step,
+// (-beta e - (1 - beta) re) - (-beta_old e - (1 - beta_old) re), re the
+// reference's log-probability of the state; with the uniform reference
+// re = 0 and only the two f32-rounded products remain (same value)
+__device__ __forceinline__ double ais_dlw(float beta, float beta_old, float e,
+                                         int n, int ones, double logp,
+                                         double log1p_, bool uniform_ref) {
+  if (uniform_ref)
+    return (double)__fmul_rn(-beta, e) - (double)__fmul_rn(-beta_old, e);
+  const double re = -((double)(n - ones) * logp + (double)ones * log1p_);
+  return ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
+         ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+}
+
 template <int NC, int GW>
 __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -96,11 +110,8 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
   for (int k = 0; k < a.num_temps; ++k) {
     const float beta = a.temps[k];
     if (a.order == 1) {
-      const float e = (float)E;
-      const double re =
-          -((double)(n - ones) * logp + (double)ones * log1p_);
-      lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
-            ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+      lw += ais_dlw(beta, beta_old, (float)E, n, ones, logp, log1p_,
+                    a.ref != 1);
     }
     const int32_t* perm =
         a.perm + ((int64_t)k * a.num_instances + inst) * a.max_n;
@@ -162,11 +173,8 @@ __global__ void __launch_bounds__(128) k_ais(const AisArgs a) {
       }
     }
     if (a.order == 0) {
-      const float e = (float)E;
-      const double re =
-          -((double)(n - ones) * logp + (double)ones * log1p_);
-      lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
-            ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+      lw += ais_dlw(beta, beta_old, (float)E, n, ones, logp, log1p_,
+                    a.ref != 1);
     }
     beta_old = beta;
   }
@@ -232,10 +240,8 @@ __global__ void __launch_bounds__(128) k_ais_small(const AisArgs a) {
   for (int k = 0; k < a.num_temps; ++k) {
     const float beta = a.temps[k];
     if (a.order == 1) {
-      const float e = (float)E;
-      const double re = -((double)(n - ones) * logp + (double)ones * log1p_);
-      lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
-            ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+      lw += ais_dlw(beta, beta_old, (float)E, n, ones, logp, log1p_,
+                    a.ref != 1);
     }
     const int32_t* perm =
         a.perm + ((int64_t)k * a.num_instances + inst) * a.max_n;
@@ -265,10 +271,8 @@ __global__ void __launch_bounds__(128) k_ais_small(const AisArgs a) {
       for (int c = 0; c < n; ++c) H[c * 128] = fmaf(d, Jr[c], H[c * 128]);
     }
     if (a.order == 0) {
-      const float e = (float)E;
-      const double re = -((double)(n - ones) * logp + (double)ones * log1p_);
-      lw += ((double)__fmul_rn(-beta, e) - (1.0 - (double)beta) * re) -
-            ((double)__fmul_rn(-beta_old, e) - (1.0 - (double)beta_old) * re);
+      lw += ais_dlw(beta, beta_old, (float)E, n, ones, logp, log1p_,
+                    a.ref != 1);
     }
     beta_old = beta;
   }

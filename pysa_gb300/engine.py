@@ -663,10 +663,15 @@ def run_ais_batch(problem_type: str, instances: list, temps: np.ndarray, *,
     batch = PTBatch(problem_type, insts, perm_slots=max(len(temps), 1),
                     kernel="plain")
     words = batch.words
-    batch.set_states(np.concatenate([
-        pack_spins(np.asarray(x0).reshape(x0.shape[0], 1, -1), problem_type,
-                   words).reshape(-1, words) for _, _, x0 in instances]),
-        None)
+    ns_all = {int(np.asarray(x0).shape[1]) for _, _, x0 in instances}
+    if len(ns_all) == 1:  # one packing call for the whole batch
+        packed = pack_spins(np.concatenate(
+            [np.asarray(x0) for _, _, x0 in instances]), problem_type, words)
+    else:
+        packed = np.concatenate([
+            pack_spins(np.asarray(x0), problem_type, words)
+            for _, _, x0 in instances])
+    batch.set_states(packed, None)
     temps_d = torch.from_numpy(temps).to(batch.device)
     C = max(batch.num_chains, 1)
     log_w = torch.zeros(C, dtype=torch.float64, device=batch.device)
@@ -685,12 +690,16 @@ def run_ais_batch(problem_type: str, instances: list, temps: np.ndarray, *,
     batch.check_status()
     spins = batch.spins.cpu().numpy().view("<u4")
     lw = log_w.cpu().numpy()
+    # one unpacking call when every instance has the same n
+    every = (unpack_spins(spins, next(iter(ns_all)), problem_type, np.float32)
+             if len(ns_all) == 1 else None)
     out = []
     for i, (_, _, x0) in enumerate(instances):
-        ns, n = x0.shape
+        ns, n = np.asarray(x0).shape
         c0 = int(batch.chain_off[i])
-        out.append((unpack_spins(spins[c0:c0 + ns], n, problem_type,
-                                 np.float32), lw[c0:c0 + ns]))
+        smp = (every[c0:c0 + ns] if every is not None else
+               unpack_spins(spins[c0:c0 + ns], n, problem_type, np.float32))
+        out.append((smp, lw[c0:c0 + ns]))
     return out
 
 
