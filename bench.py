@@ -365,33 +365,46 @@ def run_batch_workload(args, w, rank, world):
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
     attempts = float(R * Rd * sizes.sum())
-    for _ in range(args.warmup):
-        batch.run(1, seed=3, graph_chunk=0, final_recompute=False)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32,
-                        device="cuda")
+    batch.run(args.warmup, seed=3, graph_chunk=0, final_recompute=False)
     st = torch.cuda.current_stream()
-    ev = [(torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # timed: the K sweeps in one call, as the API runs them (every instance
+    # on the tensor cores: persistent launches of up to 128 sweeps with the
+    # exchange fused).  The batch's couplings (1.6 GB) and fields (5 GB)
+    # are far larger than L2, so no flush between sweeps.
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(
+        enable_timing=True)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     with sampler:
-        for k in range(args.steps):
-            flush.fill_(float(k))
-            a, b = ev[k]
-            a.record(st)
-            batch.run(1, seed=3, graph_chunk=0, final_recompute=False)
-            b.record(st)
+        a.record(st)
+        batch.run(args.steps, seed=3, graph_chunk=0, final_recompute=False)
+        b.record(st)
         torch.cuda.synchronize()
     batch.check_status()
-    ms = [a.elapsed_time(b) for a, b in ev]
-    total_s = sum(ms) / 1e3
+    total_s = a.elapsed_time(b) / 1e3
+    ms = [1e3 * total_s / args.steps]
     if dist:
         t = torch.tensor([total_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
     value = attempts * args.steps * world / total_s
+    # for comparison: one sweep per call (one launch per fold per sweep,
+    # fields through HBM every sweep), L2 flushed before each
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device="cuda")
+    ev1 = [(torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a1, b1 = ev1[k]
+        a1.record(st)
+        batch.run(1, seed=3, graph_chunk=0, final_recompute=False)
+        b1.record(st)
+    torch.cuda.synchronize()
+    one_sweep = attempts * args.steps / (
+        sum(x.elapsed_time(y) for x, y in ev1) / 1e3)
     # graph-captured chunks (the production path), one timing
     g0 = time.perf_counter()
     batch.run(128, seed=3, graph_chunk=64)
@@ -430,6 +443,16 @@ def run_batch_workload(args, w, rank, world):
                "cores": os.cpu_count() or 1, "kind": "port",
                "sample": f"median-size instance (n={n}), 8 reads x {R} "
                          f"replicas x 20 sweeps ({dt:.1f} s)"}
+    # launches in the timed call: per fold with instances, one persistent
+    # kernel and its schedule reset per launch of up to 128 sweeps (fused
+    # path); else per sweep the fold kernels, the plain variants and the
+    # exchange
+    folds = int(sum(1 for v in range(3) if batch.ws.tc_variant_count[v] > 0))
+    if batch.tc_min_n is not None and all(int(x) >= batch.tc_min_n
+                                          for x in sizes):
+        gpu_launches = folds * -(-args.steps // 128)
+    else:
+        gpu_launches = args.steps * (folds + 3 + 1)
     if rank == 0:
         hbm, bf16, kind = measured_peaks()
         print(json.dumps({
@@ -442,15 +465,17 @@ def run_batch_workload(args, w, rank, world):
                        "n_min": int(sizes.min()), "n_max": int(sizes.max()),
                        "n_sum": int(sizes.sum()), "replicas": R, "reads": Rd,
                        "chains": int(I * R * Rd),
-                       "l2": "flushed (256 MB write) before every step",
+                       "l2": "inputs larger than L2 (couplings 1.6 GB, "
+                             "fields 5 GB); the K sweeps in one call",
                        "kernel_split": {"tc_min_n": batch.tc_min_n,
                                         "autotune_ms_per_sweep":
                                             {str(k): v for k, v in tune.items()}},
                        "setup_s": setup_s},
             "graph_chunk64_value": graph_rate,
+            "one_sweep_launches_value": one_sweep,
             "roofline": None, "clocks": sampler.summary(), "e2e": e2e,
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps * (1 + 3 + 8)}), flush=True)
+            "gpu_launches": gpu_launches}), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
