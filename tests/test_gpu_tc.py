@@ -20,13 +20,13 @@ def _int_qubo(rng, n):
 
 
 def _run(ptype, J, h, betas, x0, *, seed, sweeps, kernel, update="sequential",
-         energies=None):
+         energies=None, **run_kw):
     from pysa_gb300 import Instance, PTBatch, pack_spins, unpack_spins
     Rd, R, n = x0.shape
     b = PTBatch(ptype, [Instance(J, h, betas, Rd)], kernel=kernel)
     assert b.tc == (kernel == "tc")
     b.set_states(pack_spins(x0, ptype, b.words), energies)
-    b.run(sweeps, seed=seed, update=update)
+    b.run(sweeps, seed=seed, update=update, **run_kw)
     got = b.fetch()
     got["spins_f"] = unpack_spins(got["spins"].reshape(Rd, R, -1), n, ptype,
                                   np.float32)
@@ -127,6 +127,35 @@ def test_tc_split_bf16_energy_error(oracle, n):
     e_err = np.max(np.abs(E - ref)) / scale
     f_err = np.max(np.abs(fields - f64)) / np.abs(f64).max()
     print(f"n={n}: energy rel err {e_err:.3e}, field rel err {f_err:.3e}")
+    assert e_err <= 1e-5
+    assert f_err <= 1e-5
+
+
+@pytest.mark.parametrize("n", [320, 1024, 2048])
+def test_tc_split_bf16_drift_between_recomputes(oracle, n):
+    """Three sweeps after the last in-kernel recompute (one every 4 sweeps,
+    the default, none at the end) the accumulated energies and the fields
+    stay within 1e-5 relative of FP64 from the same spins.  (Every 8 sweeps
+    does not: 1.1e-5 at n = 1024 after seven sweeps.)"""
+    rng = np.random.default_rng(7 * n)
+    J = np.triu(rng.normal(size=(n, n)) / np.sqrt(n), 1)
+    J = (J + J.T).astype(np.float32)
+    h = (0.1 * rng.normal(size=n)).astype(np.float32)
+    R, Rd = 8, 4
+    betas = (1.0 / np.geomspace(0.2, 2.0, R)).astype(np.float32)
+    x0 = (2 * rng.integers(0, 2, (Rd, R, n)) - 1).astype(np.float32)
+    got = _run("ising", J, h, betas, x0, seed=5, sweeps=199, kernel="tc",
+               recompute_every=4, final_recompute=False)
+    assert got["batch"].tc_terms == 2
+    E = got["energies"].reshape(-1)
+    S = got["spins_f"].reshape(-1, n)
+    ref = np.array([oracle.energy64(J, h, s) for s in S])
+    fields = got["batch"].fields.cpu().numpy()[:len(S), :n]
+    f64 = S.astype(np.float64) @ J.astype(np.float64) + h
+    e_err = np.max(np.abs(E - ref)) / np.abs(ref).max()
+    f_err = np.max(np.abs(fields - f64)) / np.abs(f64).max()
+    print(f"n={n}: after 3 sweeps of drift: energy rel err {e_err:.3e}, "
+          f"field rel err {f_err:.3e}")
     assert e_err <= 1e-5
     assert f_err <= 1e-5
 
