@@ -52,6 +52,8 @@ struct TcCfg {
   // F == 2: corrections of sub-blocks 2 and 3 from the older sub-blocks,
   // computed by the idle slice's threads ([2][16][CC] floats)
   static constexpr bool HELP = F == 2;
+  // F == 4: the three idle slices' warps write the A rows of sub-blocks 0-2
+  static constexpr bool APUT = F == 4;
   static constexpr size_t CORR_OFF = BETA_OFF + CC * 4;
   static constexpr size_t CORR_BYTES = HELP ? (size_t)2 * 16 * CC * 4 : 0;
   // RND, F > 1: fields of the block's 64 scattered columns, gathered by the
@@ -133,6 +135,16 @@ __device__ __forceinline__ void named_sync_128() {
 
 // Deciding and helping threads of the four decision warps (fold 2).
 __device__ __forceinline__ void named_sync_dec() {
+  __syncwarp();
+  asm volatile("barrier.sync 3, 128;" ::: "memory");
+}
+// Fold 4: the deciding warp announces sub-blocks 0-2 without waiting; the
+// three other warps wait for it (the same barrier, 128 threads in all)
+__device__ __forceinline__ void named_arrive_aput() {
+  __syncwarp();
+  asm volatile("barrier.arrive 3, 128;" ::: "memory");
+}
+__device__ __forceinline__ void named_sync_aput() {
   __syncwarp();
   asm volatile("barrier.sync 3, 128;" ::: "memory");
 }
@@ -866,6 +878,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 if (g == 3 && (Gb == G0 || tc_wait(sh.mma_done, (Gb - 1) & 1,
                                                    sh, status)))
                   put_a(3, dcur);
+              } else if constexpr (C::APUT) {
+                // sub-blocks 0-2 go to the other slices' warps; the last
+                // sub-block's rows here, after the previous block's MMAs
+                if (g == 2) named_arrive_aput();
+                if (g == 3 && (Gb == G0 || tc_wait(sh.mma_done, (Gb - 1) & 1,
+                                                   sh, status)))
+                  put_a(3, dcur);
               } else {
                 if (g == 1)
                   a_early =
@@ -880,7 +899,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               if (lead) stamp(a, Gb, 10 + 3 * g);
               if (C::HELP && g < 3) named_sync_dec();  // sub-block g published
             }
-            if (!C::HELP && !a_early) {
+            if (!C::HELP && !C::APUT && !a_early) {
               if (Gb > G0) {
                 if (lead) stamp(a, Gb, 2);
                 const bool a_ok =
@@ -919,6 +938,20 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 }
               }
               dE_s[c] += (double)dEb;
+            }
+            fence_proxy_async();
+          } else if constexpr (C::APUT) {
+            // one of the three other slices' warps (or every warp after an
+            // abort): the A rows of sub-block hr once sub-blocks 0-2 are
+            // decided and the previous block's MMAs are done
+            named_sync_aput();
+            const int hr = (q + 3 - qt) & 3;  // 0, 1, 2 for q = qt+1, +2, +3
+            if (hr < 3 && __all_sync(0xffffffffu, !*sh.abort) &&
+                (Gb == G0 || tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status))) {
+              float d[16];
+#pragma unroll
+              for (int j = 0; j < 16; ++j) d[j] = dl_s[(16 * hr + j) * CC + c];
+              put_a(hr, d);
             }
             fence_proxy_async();
           } else if (C::HELP) {
