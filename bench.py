@@ -176,7 +176,9 @@ def field_errors(batch, J, h, ptype):
     return {"field_max_abs_err": float((Hg - H).abs().max()),
             "field_max_rel_err": float((Hg - H).abs().max() / H.abs().max()),
             "energy_max_rel_err": float(((Eg - E).abs() / E.abs().clamp_min(
-                1e-30)).max())}
+                1e-30)).max()),
+            "energy_err_of_scale": float((Eg - E).abs().max() /
+                                         E.abs().max())}
 
 
 def measured_peaks():
@@ -975,6 +977,10 @@ def main():
     accuracy = None
     if w["kind"] == "wishart":
         accuracy = field_errors(batch, J, h, ptype)
+        # the energies a run returns: recomputed from the spins at its end
+        batch.recompute()
+        accuracy["returned_energy_err_of_scale"] = field_errors(
+            batch, J, h, ptype)["energy_err_of_scale"]
         _, t_pl, e_gs = planted_wishart(n, w["m"], np.random.default_rng(2024))
         rbest = batch.best_energy.view(Rd, R).min(dim=1).values.cpu().numpy()
         accuracy.update({
@@ -983,8 +989,12 @@ def main():
             "reads_at_planted": int((rbest <= e_gs + 1e-5 * abs(e_gs)).sum()),
             "sweeps_run": args.warmup + args.steps,
             "block_b": 64,
-            "note": "fields and energies after the last timed sweep "
-                    "(in-kernel FP64-accumulated recompute every 4 sweeps)"})
+            "note": "fields and energies after the last timed sweep, "
+                    "accumulated since the last in-kernel recompute (every "
+                    "4 sweeps, compensated f32 sums); per-chain relative "
+                    "(energy_max_rel_err) and relative to the largest |E| "
+                    "(energy_err_of_scale); returned_*: after the final "
+                    "recompute a run ends with"})
     # per-sweep kernel time (fused launches include their exchange)
     sweep_ms = [a.elapsed_time(b) / cnt for (a, b, _), cnt in zip(ev, iters)]
     step_ms = [a.elapsed_time(c) / cnt for (a, _, c), cnt in zip(ev, iters)]
