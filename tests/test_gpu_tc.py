@@ -4,7 +4,7 @@ Integer couplings are exact in BF16 and every FP32 sum stays below 2^24, so
 trajectories must match the oracle (the reference's dense-dot rule on the same
 Philox stream) bit for bit.  Real couplings take the split J_hi + J_lo path;
 their energies are checked against an FP64 recomputation of the returned
-states with the tolerance the spec workload sets (1e-5 relative).
+states with the tolerance the split-BF16 path promises (1e-5 relative).
 """
 import numpy as np
 import pytest
