@@ -21,9 +21,13 @@
 // 1-D bulk copies (TMA engine).  Integer couplings make every product and sum
 // exact, so trajectories match the plain sweep bit for bit.
 //
-// Roles: warps 0-3 decide (thread = TMEM lane), warp 4 issues MMAs, warp 5
-// produces stages, warps 6-7 precompute the next block's log-uniforms.  Every wait is bounded; a timeout sets the status word and
-// an abort flag that releases every other wait.
+// Roles: warps 0-3 decide (thread = TMEM lane; with F > 1 only the warps of
+// the slice holding the block's columns, the others help: at F = 2 they
+// compute the older sub-blocks' corrections and write A rows, at F = 4 they
+// write A rows), warp 4 issues MMAs, warp 5 produces stages, warps 6-7
+// precompute the next block's log-uniforms.  Every wait is bounded; a
+// timeout sets the status word and an abort flag that releases every other
+// wait.
 #include "aux.cuh"
 #include "tc_api.h"
 #include "tc_ptx.cuh"
