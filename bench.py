@@ -97,7 +97,14 @@ def ladder(w):
 
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples around and during the timed region.
+
+    A timed region of a few milliseconds ends before `nvidia-smi -lms`
+    prints its first line, so entering waits (up to 10 s) for a first sample
+    and leaving waits for one taken after the region ended; the summary keeps
+    the samples from the last one before the region to the first one after
+    it.  When the looping form prints nothing, single queries are polled
+    instead.  Only reads clocks; changes no setting."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
               "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -108,41 +115,94 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []   # (time, line)
+        self.mode = None
+        self._stop = threading.Event()
+        self._got = threading.Event()
+        self.t_in = self.t_out = None
 
-    def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index),
-                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE,
-                stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except (OSError, FileNotFoundError):
-            self.proc = None
-        return self
+    def _cmd(self, loop):
+        c = ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+             "--format=csv,noheader,nounits"]
+        return c + (["-lms", "100"] if loop else [])
+
+    def _add(self, line):
+        line = line.strip()
+        if len(line.split(",")) >= 9:
+            self.lines.append((time.perf_counter(), line))
+            self._got.set()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self._add(line)
+            if self._stop.is_set():
+                break
 
-    def __exit__(self, *a):
+    def _poll(self):
+        while not self._stop.is_set():
+            try:
+                r = subprocess.run(self._cmd(False), capture_output=True,
+                                   text=True, timeout=5)
+                for line in r.stdout.splitlines():
+                    self._add(line)
+            except (OSError, subprocess.TimeoutExpired):
+                return
+            self._stop.wait(0.1)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(self._cmd(True),
+                                         stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.mode = "loop"
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            if not self._got.wait(5.0):
+                self._end_proc()
+                self.mode = "poll"
+                self.t = threading.Thread(target=self._poll, daemon=True)
+                self.t.start()
+                self._got.wait(5.0)
+        except (OSError, FileNotFoundError):
+            self.proc, self.mode = None, None
+        self.t_in = time.perf_counter()
+        return self
+
+    def _end_proc(self):
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.proc = None
+
+    def __exit__(self, *a):
+        self.t_out = time.perf_counter()
+        if self.mode:
+            deadline = self.t_out + 5.0
+            while time.perf_counter() < deadline and not any(
+                    t > self.t_out for t, _ in self.lines):
+                time.sleep(0.02)
+        self._stop.set()
+        self._end_proc()
 
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.t_in is not None and self.t_out is not None and lines:
+            before = [k for k, (t, _) in enumerate(lines) if t <= self.t_in]
+            after = [k for k, (t, _) in enumerate(lines) if t >= self.t_out]
+            lo = before[-1] if before else 0
+            hi = after[0] if after else len(lines) - 1
+            lines = lines[lo:hi + 1]
+        inside = sum(1 for t, _ in lines
+                     if self.t_in is not None and self.t_out is not None and
+                     self.t_in < t < self.t_out)
+        for _, ln in lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
             try:
                 sm.append(float(parts[1]))
                 mx.append(float(parts[2]))
@@ -153,9 +213,12 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
-                    "samples": 0}
+                    "samples": 0, "mode": self.mode}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "samples_inside": inside, "mode": self.mode,
+                "window": "last sample before the timed region to the first "
+                          "after it"}
 
 
 def field_errors(batch, J, h, ptype):
@@ -1087,10 +1150,30 @@ def main():
         # energies, slots, best energies and sweeps
         h2d = 4 * n * n + 4 * n + 4 * R + C * n * 4
         d2h = C * (n * 4 + words * 4 * 2 + 4 * 4)
+        # the returned energies must be the energies of the returned states
+        # (f64 recomputation, pysa/qubo.py:32-37; exact for integer QUBO)
+        Jd = torch.from_numpy(J.astype(np.float64)).cuda()
+        hd = torch.from_numpy(h.astype(np.float64)).cuda()
+        S = torch.from_numpy(np.stack([r["states"] for r in rows]).reshape(
+            -1, n).astype(np.float64)).cuda()
+        Ef = (S * (0.5 * (S @ Jd) + hd)).sum(1).cpu().numpy()
+        Eg = np.concatenate([r["energies"] for r in rows]).astype(np.float64)
+        e_err = float(np.max(np.abs(Eg - Ef)) / max(np.abs(Ef).max(), 1.0))
+        tol = 0.0 if w["kind"] == "qubo" else 1e-5
+        if e_err > tol:
+            raise AssertionError(f"e2e: returned energies differ from the "
+                                 f"returned states' energies ({e_err:.3e})")
+        del S, Jd, hd
+        # a step is one sweep: the call's copies amortised over its sweeps
         e2e = {"value": Rd * R * n * sweeps_e2e / e2e_s, "unit": "attempts/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "h2d_bytes_per_step": int(h2d // sweeps_e2e),
+               "d2h_bytes_per_step": int(d2h // sweeps_e2e),
+               "h2d_bytes_per_call": int(h2d), "d2h_bytes_per_call": int(d2h),
                "sweeps_per_call": sweeps_e2e, "seconds": e2e_s,
-               "best_energy_min": float(min(r["best_energy"] for r in rows))}
+               "best_energy_min": float(min(r["best_energy"] for r in rows)),
+               "energy_check": {"max_err_of_scale": e_err, "tolerance": tol,
+                                "against": "f64 energies of the returned "
+                                           "states"}}
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:

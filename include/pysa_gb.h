@@ -231,6 +231,14 @@ const char *pysa_gb_last_error(void);
  * script).  No counterpart in the reference. */
 int pysa_gb_set_trace(void *device_buffer);
 
+/* Diagnostics: bound, in nanoseconds, of the tensor-core sweep's wait for a
+ * work item's previous unit (0 restores the default of one second).  A
+ * unit waits only at its start, with nothing in flight, so a tiny bound
+ * makes a run end cleanly with PYSA_GB_ERR_TIMEOUT in the status word: the
+ * way tests exercise the timeout path.  Applies to launches enqueued after
+ * the call, process-wide.  No counterpart in the reference. */
+int pysa_gb_set_unit_wait_limit(uint64_t ns);
+
 /* Workspace sizing and set-up.
  *   pysa_gb_workspace_bytes: sizes of the workspace arrays for a batch
  *     described by host tables (n, replicas, reads are read); returns the
@@ -288,8 +296,12 @@ int pysa_gb_sweeps(const pysa_gb_problems *p, pysa_gb_state *s,
  * spins and resets best_*; 0 continues from the caller's energies and best_*.
  * Fields are rebuilt from the spins on every call.  All calls share the
  * array: calls that overlap on the GPU race.  The first call on each device
- * resolves the array's address and should come before any stream capture.
- * Sequential and random order; never the tensor-core kernel. */
+ * resolves the array's address and should come before any stream capture;
+ * the address stays cached, so after cudaDeviceReset the entry point must
+ * not be called again on that device.  Dense couplings only: a batch with a
+ * sparse-row instance (host->sparse) is rejected with PYSA_GB_ERR_ARG
+ * before anything is enqueued.  Sequential and random order; never the
+ * tensor-core kernel. */
 int pysa_gb_sweeps_noalloc(const pysa_gb_problems *p, pysa_gb_state *s,
                            const pysa_gb_host_tables *host,
                            const pysa_gb_options *o, int32_t init,

@@ -10,6 +10,7 @@ bit for bit with the CUDA path on integer couplings:
 
   pt_run          simulation_parallel / simulation_sequential + utils.pt
                   (pysa/simulation.py:123-236, pysa/utils.py:26-58)
+  pt_run64        the same in f64 (float_type='float64', pysa/sa.py:204-205)
   ais_run         ais_sample + update_spin_ref (pysa/simulation.py:293-317,
                   pysa/ising.py:66-92, pysa/qubo.py:66-92)
   energy64        get_energy (pysa/ising.py:32-37) in f64
@@ -60,6 +61,14 @@ class _PtState(ctypes.Structure):
                 ("lo_stride", ctypes.c_int32)]
 
 
+class _PtState64(ctypes.Structure):
+    _fields_ = [("spins", ctypes.c_void_p), ("energies", ctypes.c_void_p),
+                ("beta_idx", ctypes.c_void_p),
+                ("best_energy", ctypes.c_void_p),
+                ("best_sweep", ctypes.c_void_p),
+                ("best_spins", ctypes.c_void_p)]
+
+
 class _AisArgs(ctypes.Structure):
     _fields_ = [("problem_type", ctypes.c_int32), ("n", ctypes.c_int32),
                 ("ld", ctypes.c_int32), ("num_temps", ctypes.c_int32),
@@ -88,6 +97,11 @@ def lib():
             ctypes.c_int
         ]
         _lib.orc_pt_run.restype = ctypes.c_int
+        _lib.orc_pt_run64.argtypes = [
+            ctypes.POINTER(_PtArgs), P, P, P, ctypes.POINTER(_PtState64),
+            ctypes.c_int64, ctypes.c_int32, ctypes.c_int
+        ]
+        _lib.orc_pt_run64.restype = ctypes.c_int
         _lib.orc_ais_run.argtypes = [
             ctypes.POINTER(_AisArgs), P, P, P, P, P, ctypes.c_int
         ]
@@ -203,6 +217,46 @@ def pt_run(problem_type: str,
                 best_sweep=bs,
                 best_spins=bsp,
                 log_omega=lo[:, first_sweep:] if log_omega else None)
+
+
+def pt_run64(problem_type: str,
+             J: np.ndarray,
+             h: np.ndarray,
+             betas: np.ndarray,
+             spins: np.ndarray,
+             energies: np.ndarray,
+             beta_idx: np.ndarray,
+             *,
+             seed: int,
+             num_sweeps: int,
+             first_sweep: int = 0,
+             update: str = "sequential",
+             use_pt: bool = True,
+             inst: int = 0,
+             nthreads: int = 0):
+    """The PT driver in f64 throughout: the reference's arithmetic for a
+    Solver built with float_type='float64' (pysa/sa.py:204-205).  Same
+    stream and arguments as pt_run (per-replica best); arrays in f64."""
+    J = np.ascontiguousarray(J, np.float64)
+    h = np.ascontiguousarray(h, np.float64)
+    betas = np.ascontiguousarray(betas, np.float64)
+    reads, R, n = spins.shape
+    sp = np.ascontiguousarray(spins, np.float64).copy()
+    en = np.ascontiguousarray(energies, np.float64).copy()
+    bi = np.ascontiguousarray(beta_idx, np.int32).copy()
+    be, bs, bsp = en.copy(), np.zeros_like(bi), sp.copy()
+    args = _PtArgs(0 if problem_type == "ising" else 1, n, J.shape[1], R,
+                   reads, inst, 1 if update == "random" else 0, int(use_pt),
+                   0, 0, seed & ((1 << 64) - 1))
+    st = _PtState64(sp.ctypes.data, en.ctypes.data, bi.ctypes.data,
+                    be.ctypes.data, bs.ctypes.data, bsp.ctypes.data)
+    rc = lib().orc_pt_run64(ctypes.byref(args), _p(J), _p(h), _p(betas),
+                            ctypes.byref(st), first_sweep, num_sweeps,
+                            nthreads)
+    if rc != 0:
+        raise MemoryError("oracle pt_run64 failed")
+    return dict(spins=sp, energies=en, beta_idx=bi, best_energy=be,
+                best_sweep=bs, best_spins=bsp)
 
 
 # ---------------------------------------------------------------------- AIS

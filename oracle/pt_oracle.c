@@ -23,6 +23,8 @@
  *   pysa/simulation.py:293-317                ais_sample
  *   pysa/utils.py:26-58                       pt (replica exchange of beta_idx)
  *   pysa/ais.py:79-112                        get_log_omega
+ *   pysa/sa.py:204-205                         float_type='float64' runs
+ *                                              (orc_pt_run64, f64 throughout)
  *
  * Numeric spec (identical on the GPU):
  *   u(x)      = (x + 0.5) * 2^-32 for a Philox output word x  (exact in f64)
@@ -268,6 +270,112 @@ int orc_pt_run(const orc_pt_args *a, const float *J, const float *h,
       if (a->log_omega)
         st->log_omega[(int64_t)rd * st->lo_stride + sw] =
             log_omega_of(R, betas, sorted_slots, bidx, E);
+    }
+  }
+  free(perm);
+  free(cbeta);
+  return 0;
+}
+
+/* --------------------------------------------- PT driver in f64 (batch) */
+/* The same driver with the arithmetic the reference uses when the Solver is
+ * built with float_type='float64' (pysa/sa.py:204-205 casts couplings, fields,
+ * states and betas to it): f64 couplings and states, field J_pos.s + h_pos in
+ * f64 (pysa/ising.py:48-49, pysa/qubo.py:48-49), dn and the acceptance test
+ * in f64, f64 energies, exchange with de = (E1 - E2)(b1 - b2) in f64
+ * (pysa/utils.py:44-58).  Same random stream and visiting orders as
+ * orc_pt_run; per-replica best (simulation_parallel). */
+typedef struct {
+  double *spins, *energies;
+  int32_t *beta_idx;
+  double *best_energy;
+  int32_t *best_sweep;
+  double *best_spins;
+} orc_pt_state64;
+
+static inline double dot8_64(const double *a, const double *b, int n) {
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int j = 0;
+  for (; j + 8 <= n; j += 8)
+    for (int k = 0; k < 8; ++k) acc[k] += a[j + k] * b[j + k];
+  for (; j < n; ++j) acc[j & 7] += a[j] * b[j];
+  double s = 0.0;
+  for (int k = 0; k < 8; ++k) s += acc[k];
+  return s;
+}
+
+int orc_pt_run64(const orc_pt_args *a, const double *J, const double *h,
+                 const double *betas, orc_pt_state64 *st, int64_t first_sweep,
+                 int32_t num_sweeps, int nthreads) {
+  const int n = a->n, R = a->replicas, Rd = a->reads;
+  const int64_t C = (int64_t)R * Rd;
+  int32_t *perm = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  double *cbeta = (double *)malloc(sizeof(double) * (size_t)(C > 0 ? C : 1));
+  if (!perm || !cbeta) {
+    free(perm);
+    free(cbeta);
+    return -1;
+  }
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  (void)nthreads;
+#endif
+  for (int64_t sw = first_sweep; sw < first_sweep + num_sweeps; ++sw) {
+    uint32_t sweep = (uint32_t)sw;
+    if (a->update == 1) orc_permutation(a->seed, a->inst, sweep, n, perm);
+    for (int rd = 0; rd < Rd; ++rd)
+      for (int k = 0; k < R; ++k)
+        cbeta[(int64_t)rd * R + st->beta_idx[(int64_t)rd * R + k]] = betas[k];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (int64_t c = 0; c < C; ++c) {
+      double *sp = st->spins + c * n;
+      double dE = 0.0;
+      for (int t = 0; t < n; ++t) {
+        const int pos = (a->update == 1) ? perm[t] : t;
+        const uint32_t x = orc_draw(a->seed, ORC_TAG_SWEEP, a->inst, sweep,
+                                    (uint32_t)c, (uint32_t)t);
+        const double field = dot8_64(J + (size_t)pos * a->ld, sp, n) + h[pos];
+        const double dn = (a->problem_type == ORC_ISING)
+                              ? 2.0 * sp[pos] * field
+                              : (2.0 * sp[pos] - 1.0) * field;
+        int acc = dn >= 0.0;
+        if (!acc) acc = log(u_of(x)) < cbeta[c] * dn;
+        if (!acc) continue;
+        if (a->problem_type == ORC_ISING)
+          sp[pos] = -sp[pos];
+        else
+          sp[pos] = (sp[pos] != 0.0) ? 0.0 : 1.0;
+        dE -= dn;
+      }
+      st->energies[c] += dE;
+      if (st->energies[c] < st->best_energy[c]) {
+        st->best_energy[c] = st->energies[c];
+        st->best_sweep[c] = (int32_t)sw;
+        memcpy(st->best_spins + c * n, sp, sizeof(double) * (size_t)n);
+      }
+    }
+    if (!a->use_pt) continue;
+    for (int rd = 0; rd < Rd; ++rd) {
+      int32_t *bidx = st->beta_idx + (int64_t)rd * R;
+      const double *E = st->energies + (int64_t)rd * R;
+      for (int k = 0; k < R - 1; ++k) {
+        const int k1 = R - k - 1, k2 = R - k - 2;
+        const double de = (E[bidx[k1]] - E[bidx[k2]]) * (betas[k1] - betas[k2]);
+        int swap = de >= 0.0;
+        if (!swap) {
+          const uint32_t x =
+              orc_draw(a->seed, ORC_TAG_PT, a->inst, sweep, (uint32_t)rd, k);
+          swap = u_of(x) < exp(de);
+        }
+        if (swap) {
+          const int32_t t = bidx[k1];
+          bidx[k1] = bidx[k2];
+          bidx[k2] = t;
+        }
+      }
     }
   }
   free(perm);

@@ -50,6 +50,7 @@ PlainItemPlan make_item_plan() {
 
 static thread_local std::string g_last_error;
 static unsigned long long* g_tc_trace = nullptr;  // diagnostics, see below
+static uint64_t g_unit_wait_ns = 0;  // diagnostics: 0 = the default bound
 
 static int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -128,6 +129,11 @@ using namespace pysa_gb;
 extern "C" {
 
 int pysa_gb_abi_version(void) { return PYSA_GB_ABI_VERSION; }
+
+int pysa_gb_set_unit_wait_limit(uint64_t ns) {
+  g_unit_wait_ns = ns;
+  return PYSA_GB_OK;
+}
 
 int pysa_gb_set_trace(void* device_buffer) {
   g_tc_trace = reinterpret_cast<unsigned long long*>(device_buffer);
@@ -458,6 +464,35 @@ int pysa_gb_prepare(const pysa_gb_problems* p, pysa_gb_state* s,
   return PYSA_GB_OK;
 }
 
+// Sweeps per work unit for a fused launch of `chunk` sweeps over `items`
+// work items: a divisor of chunk between 4 and 16 with the shortest
+// estimated launch.  A unit costs its sweeps plus about 0.2 of a sweep to
+// move the fields between HBM and tensor memory (measured on the 1024-spin
+// QUBO workload: 8-sweep units 195 us per sweep, 1-sweep units 228); the
+// launch takes as many unit times as the waves of units over the SMs, and
+// at least the units of one item (they run one after another).  Without
+// such a divisor, `pref` (the rest goes to the next launch).  128 sweeps
+// over 256 items give 8, 20 sweeps give 5 (one launch instead of 16 + 4),
+// 128 sweeps of a single item 16.
+static int tc_unit_for(int chunk, int pref, int items, int sms) {
+  if (chunk <= pref) return chunk;
+  double best = 0.0;
+  int pick = 0;
+  for (int ku = 4; ku <= 16; ++ku) {
+    if (chunk % ku) continue;
+    const int64_t per_item = chunk / ku;
+    const int64_t units = (int64_t)items * per_item;
+    int64_t waves = (units + sms - 1) / sms;
+    if (waves < per_item) waves = per_item;
+    const double cost = (double)waves * (ku + 0.2);
+    if (pick == 0 || cost < best - 1e-9) {
+      best = cost;
+      pick = ku;
+    }
+  }
+  return pick ? pick : pref;
+}
+
 int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
                    pysa_gb_workspace* ws, const pysa_gb_options* o,
                    int32_t num_sweeps, void* stream) {
@@ -528,6 +563,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.recompute_every = o->recompute_every;
   ta.use_pt = o->use_pt;
   ta.pad_ = 0;
+  ta.unit_wait_ns = g_unit_wait_ns;
   ta.sched = ws->tc_sched;
   ta.perm = ws->perm;
   ta.perm_slots = a.perm_slots;
@@ -586,10 +622,16 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
         ws->tc_launch_sweeps > 0 ? ws->tc_launch_sweeps : kMaxFusedSweeps;
     if (random && per_launch > ws->tc_rand_slots)
       per_launch = ws->tc_rand_slots;
+    // items of the largest fold: its launch sets the number of unit waves
+    int items = 1;
+    for (int v = 0; v < 3; ++v)
+      if (ws->tc_variant_count[v] > items) items = ws->tc_variant_count[v];
     int remaining = num_sweeps;
     while (remaining > 0) {
       int chunk = remaining < per_launch ? remaining : per_launch;
-      const int ku = chunk < ku_pref ? chunk : ku_pref;
+      const int ku = ws->tc_unit_sweeps > 0
+                         ? (chunk < ku_pref ? chunk : ku_pref)
+                         : tc_unit_for(chunk, ku_pref, items, sms);
       chunk = chunk / ku * ku;
       if (random) {
         const int rc = rand_prepare(chunk);

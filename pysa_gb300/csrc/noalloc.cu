@@ -18,8 +18,15 @@
 //     threads without ordering) race on the array.
 //   * The first call on each device resolves the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
-//   * It allocates nothing: no cudaMalloc / cudaFree, no host heap.
+//     before any stream capture.  The address is cached for the life of the
+//     process: cudaDeviceReset (or anything else that re-creates the
+//     device's primary context) leaves it stale, so do not call this entry
+//     point again on a device after resetting it.
+//   * Dense couplings only: a batch with a sparse-row instance
+//     (pysa_gb_host_tables.sparse) is rejected before anything is enqueued.
+//   * It allocates nothing: no cudaMalloc / cudaFree, no host heap.  The
+//     work list is rebuilt on the device on every call by one CTA in
+//     O(instances / 256 + log 256) steps.
 #include <mutex>
 
 #include "aux.cuh"
@@ -53,35 +60,69 @@ static int noalloc_scratch(void** out) {
   return PYSA_GB_OK;
 }
 
-// Work list on the device: thread per instance; its items start after the
-// items of the earlier instances of the same kernel variant.
-__global__ void k_noalloc_items(const int32_t* n, const int32_t* replicas,
-                                const int32_t* reads, const int64_t* chain_off,
-                                int num_instances, PlainItemPlan plan,
-                                SweepItem* items) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= num_instances) return;
-  const int v = plan.variant_of(n[i]);
-  int64_t pos = plan.start[v];
-  int64_t poff = 0;
-  for (int j = 0; j < i; ++j) {
-    const int vj = plan.variant_of(n[j]);
-    poff += (int64_t)n[j] * plan.row_floats[vj];
-    if (vj == v)
-      pos += ((int64_t)replicas[j] * reads[j] + plan.cpb[v] - 1) / plan.cpb[v];
+// Work list on the device, built by one CTA: thread t owns a contiguous
+// segment of instances; the segments' item counts (per kernel variant) and
+// packed-coupling sizes are scanned across the CTA in shared memory, then
+// every thread writes its segment's items from those starts.
+constexpr int kItemThreads = 256;
+
+__global__ void __launch_bounds__(kItemThreads)
+    k_noalloc_items(const int32_t* n, const int32_t* replicas,
+                    const int32_t* reads, const int64_t* chain_off,
+                    int num_instances, PlainItemPlan plan, SweepItem* items) {
+  constexpr int NV = kNumPlainVariants;
+  __shared__ int64_t s_sum[NV + 1][kItemThreads];  // items per variant, floats
+  const int t = threadIdx.x;
+  const int per = (num_instances + kItemThreads - 1) / kItemThreads;
+  const int i0 = min(t * per, num_instances);
+  const int i1 = min(i0 + per, num_instances);
+  auto items_of = [&](int i, int v) {
+    return ((int64_t)replicas[i] * reads[i] + plan.cpb[v] - 1) / plan.cpb[v];
+  };
+  for (int v = 0; v <= NV; ++v) s_sum[v][t] = 0;
+  for (int i = i0; i < i1; ++i) {
+    const int v = plan.variant_of(n[i]);
+    s_sum[v][t] += items_of(i, v);
+    s_sum[NV][t] += (int64_t)n[i] * plan.row_floats[v];
   }
-  const int64_t chains = (int64_t)replicas[i] * reads[i];
-  for (int64_t c = 0; c < chains; c += plan.cpb[v], ++pos) {
-    SweepItem it;
-    it.inst = i;
-    it.chain0 = (int32_t)(chain_off[i] + c);
-    it.nchains = (int32_t)((chains - c) < plan.cpb[v] ? (chains - c)
-                                                       : plan.cpb[v]);
-    it.variant = v;
-    it.poff_lo = (int32_t)(uint32_t)(poff & 0xffffffffll);
-    it.poff_hi = (int32_t)(poff >> 32);
-    it.pad0 = it.pad1 = 0;
-    items[pos] = it;
+  __syncthreads();
+  for (int off = 1; off < kItemThreads; off <<= 1) {  // inclusive scans
+    int64_t add[NV + 1];
+#pragma unroll
+    for (int v = 0; v <= NV; ++v) add[v] = t >= off ? s_sum[v][t - off] : 0;
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v <= NV; ++v) s_sum[v][t] += add[v];
+    __syncthreads();
+  }
+  int64_t pos[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    pos[v] = plan.start[v] + (t > 0 ? s_sum[v][t - 1] : 0);
+  int64_t poff = t > 0 ? s_sum[NV][t - 1] : 0;
+  for (int i = i0; i < i1; ++i) {
+    const int v = plan.variant_of(n[i]);
+    const int64_t chains = (int64_t)replicas[i] * reads[i];
+    int64_t p = 0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (k == v) p = pos[k];
+    for (int64_t c = 0; c < chains; c += plan.cpb[v], ++p) {
+      SweepItem it;
+      it.inst = i;
+      it.chain0 = (int32_t)(chain_off[i] + c);
+      it.nchains = (int32_t)((chains - c) < plan.cpb[v] ? (chains - c)
+                                                         : plan.cpb[v]);
+      it.variant = v;
+      it.poff_lo = (int32_t)(uint32_t)(poff & 0xffffffffll);
+      it.poff_hi = (int32_t)(poff >> 32);
+      it.pad0 = it.pad1 = 0;
+      items[p] = it;
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      if (k == v) pos[k] = p;
+    poff += (int64_t)n[i] * plan.row_floats[v];
   }
 }
 
@@ -100,6 +141,15 @@ extern "C" int pysa_gb_sweeps_noalloc(const pysa_gb_problems* p,
       !host->chain_off || !host->j_off || !host->ld)
     return pysa_gb_internal_fail(PYSA_GB_ERR_ARG,
                                  "sweeps_noalloc: null argument");
+  // dense couplings only: the sizes below have no room for the sparse-row
+  // kernel's layout, so such a batch is refused before anything is enqueued
+  if (host->sparse)
+    for (int i = 0; i < p->num_instances; ++i)
+      if (host->sparse[i])
+        return pysa_gb_internal_fail(
+            PYSA_GB_ERR_ARG,
+            "sweeps_noalloc: sparse-row instances are not supported (dense "
+            "couplings only); use pysa_gb_sweeps with a workspace");
   int64_t need[3];
   const int items_n = pysa_gb_workspace_bytes(p->num_instances, host, need);
   if (items_n < 0) return items_n;
@@ -150,7 +200,7 @@ extern "C" int pysa_gb_sweeps_noalloc(const pysa_gb_problems* p,
     acc += counts[v];
   }
   if (p->num_instances > 0) {
-    k_noalloc_items<<<(p->num_instances + 127) / 128, 128, 0, st>>>(
+    k_noalloc_items<<<1, kItemThreads, 0, st>>>(
         p->n, p->replicas, p->reads, p->chain_off, p->num_instances, plan,
         reinterpret_cast<SweepItem*>(ws.items));
   }

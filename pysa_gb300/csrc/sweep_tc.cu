@@ -74,8 +74,8 @@ struct TcCfg {
   static constexpr size_t POSB_BYTES = RND ? (size_t)2 * 2 * CC * 4 : 0;
   static constexpr size_t BAR_OFF = (POSB_OFF + POSB_BYTES + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
-  // lf_full[2], lf_free[2], full[NS], free[NS]
-  static constexpr int NBARS = 13 + 2 * NS;
+  // lf_full[2], lf_free[2], full[NS], free[NS], drain
+  static constexpr int NBARS = 14 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
   // tmem slot, abort flag, current unit
   static constexpr size_t BYTES = MISC_OFF + 24;
@@ -84,7 +84,7 @@ struct TcCfg {
 
 struct TcShared {
   uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *rc_full,
-      *rc_done, *lf_full, *lf_free, *full, *free_;
+      *rc_done, *lf_full, *lf_free, *full, *free_, *drain;
   uint32_t* tmem_slot;
   volatile int32_t* abort;
 };
@@ -102,6 +102,18 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity,
       return false;
     }
   }
+}
+
+// After an abort: wait (bounded, about a second, whatever the abort flag
+// says) for a barrier phase that only asynchronous work already issued by
+// this CTA completes -- bulk copies landing in shared memory, MMAs writing
+// tensor memory -- so that none is in flight when the CTA frees its tensor
+// memory and exits.
+__device__ __forceinline__ void drain_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return;
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer_ns() - t0 > 1000000000ull) return;
 }
 
 // (sum, compensation) + x with Neumaier's compensated summation in f32
@@ -288,6 +300,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   sh.lf_free = bars + 11;
   sh.full = bars + 13;
   sh.free_ = bars + 13 + C::NS;
+  sh.drain = bars + 13 + 2 * C::NS;
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
   volatile int32_t* unit_s =
@@ -366,9 +379,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           const int it = un % a.num_items, ch = un / a.num_items;
           volatile int32_t* done = a.sched + 2 + it;
           if (*done < ch) {
+            const uint64_t lim =
+                a.unit_wait_ns ? a.unit_wait_ns : 1000000000ull;
             const uint64_t t0 = globaltimer_ns();
             while (*done < ch) {
-              if (globaltimer_ns() - t0 > 1000000000ull) {
+              if (globaltimer_ns() - t0 > lim) {
                 set_status(status, PYSA_GB_ERR_TIMEOUT);
                 *sh.abort = 1;
                 un = -1;
@@ -406,6 +421,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     };
     int n_rc = 0;
     for (int s = 0; s < KU; ++s) n_rc += rc_at(s) ? 1 : 0;
+    // producer lane: ring stages issued before this unit, last diagonal
+    // block issued in it (for the drain after an abort)
+    const uint32_t u_first = u;
+    uint32_t jbb_last = 0xFFFFFFFFu;
 
     // ------------------------------------------------ unit prologue
     for (int i = threadIdx.x; i < CC * C::WORDS; i += blockDim.x) {
@@ -1317,7 +1336,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           ++u;
           return true;
         };
-        bool ok = issue_jbb(G0);
+        auto issue_jbb_t = [&](uint32_t Gx) {
+          const bool r = issue_jbb(Gx);
+          if (r) jbb_last = Gx;
+          return r;
+        };
+        bool ok = issue_jbb_t(G0);
         for (int s = 0; s < KU && ok; ++s) {
           if (rc_at(s)) {
             for (int t = 0; t < NB && ok; ++t)
@@ -1332,7 +1356,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           for (int t = 0; t < NB && ok; ++t) {
             const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
             // the next block's diagonal block lands while this one is decided
-            if (Gb + 1 < Gend) ok = issue_jbb(Gb + 1);
+            if (Gb + 1 < Gend) ok = issue_jbb_t(Gb + 1);
             const bool has_next = Gb + 1 < Gend;
             const int tn = (t + 1) % NB;
             const int jf = has_next ? ((64 * tn) % S) / 256 : 0;
@@ -1417,6 +1441,34 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    if (*sh.abort) {
+      // Aborted (a bounded wait ran out): every role has stopped issuing.
+      // Asynchronous work already in flight lands before the CTA frees its
+      // tensor memory and exits (the next unit-queue step ends it): the
+      // MMAs issued so far, and the producer's last NS ring stages and last
+      // two diagonal blocks (older copies were waited for before their
+      // buffers were reused).
+      if (warp == 4 && lane == 0) {
+        tc::commit(sh.drain);
+        drain_wait(sh.drain, 0);
+      }
+      if (warp == 5 && lane == 0) {
+        const uint32_t lo =
+            u - u_first > (uint32_t)C::NS ? u - (uint32_t)C::NS : u_first;
+        for (uint32_t x = lo; x < u; ++x)
+          drain_wait(&sh.full[x % C::NS], (x / C::NS) & 1);
+        if (jbb_last != 0xFFFFFFFFu) {
+          drain_wait(&sh.jbb_full[jbb_last & 1], (jbb_last >> 1) & 1);
+          if (jbb_last > G0)
+            drain_wait(&sh.jbb_full[(jbb_last - 1) & 1],
+                       ((jbb_last - 1) >> 1) & 1);
+        }
+      }
+      __syncwarp();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+    }
     if (threadIdx.x == 0) {
       stamp_cta(a, 4);
       __threadfence();  // this unit's stores before its done flag

@@ -32,6 +32,8 @@ struct TcArgs {
   int32_t use_pt;
   int32_t advance_counter;  // 1: the last CTA advances the sweep counter
   int32_t pad_;
+  uint64_t unit_wait_ns;  // bound of the wait for an item's previous unit
+                          // (0: one second)
   int32_t* sched;  // zeroed per launch: [0] unit queue, [1] finished CTAs,
                    // [2 + item] units of the item done
   // random order: permutation of (inst, sweep) at

@@ -176,9 +176,11 @@ def geometric_betas(R, tmin, tmax):
 # ----------------------------------------------------------------- cases
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("PYSA_REFERENCE",
-                                                          "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("PYSA_REFERENCE"),
+                    help="nasa/PySA source tree (or $PYSA_REFERENCE)")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("--reference (or PYSA_REFERENCE) is required")
     sys.path[:0] = [os.path.join(REPO, "oracle", "stubs"), args.reference]
     import sitecustomize  # noqa: F401  (np.alltrue alias for NumPy 2)
     import pysa.ising as ising

@@ -43,9 +43,11 @@ class Dense(np.ndarray):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("PYSA_REFERENCE",
-                                                          "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("PYSA_REFERENCE"),
+                    help="nasa/PySA source tree (or $PYSA_REFERENCE)")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("--reference (or PYSA_REFERENCE) is required")
     env = notebook_functions(os.path.join(args.reference, "tutorials",
                                           "hpo_demo.ipynb"))
     out = {}

@@ -1,0 +1,122 @@
+"""The exact code path of the headline measurement, bit for bit against the
+CPU oracle.
+
+The dense-QUBO workload (n = 1024, Q_ij integers in [-8, 8], diagonal in
+[-16, 16], 64 replicas on a geometric 0.5-8.0 temperature ladder) runs on the
+persistent tensor-core sweep at fold 2 (64 chains per CTA).  R = 64 divides
+the chains per CTA, so the replica exchange runs inside the kernel and one
+launch covers up to 128 sweeps in work units of 8.  These tests drive that
+path -- fused exchange, unit boundaries, launch boundaries, the short tail
+units of a run whose length is not a multiple of 8, and CUDA-graph replays --
+and compare every returned array with the oracle (pysa/simulation.py:150-171,
+pysa/qubo.py:40-63, pysa/utils.py:44-58 on the shared Philox stream).
+Integer couplings make every product and sum exact, so equality is required.
+The same at fold 4 (n = 1300, 32 chains per CTA, R = 32).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _qubo(rng, n):
+    Q = np.triu(rng.integers(-8, 9, (n, n)), 1)
+    Q = (Q + Q.T).astype(np.float32)
+    return Q, rng.integers(-16, 17, n).astype(np.float32)
+
+
+def _ising_pm1(rng, n):
+    P = np.triu(2 * rng.integers(0, 2, (n, n)) - 1, 1)
+    return (P + P.T).astype(np.float32), np.zeros(n, np.float32)
+
+
+def _check_equal(got, want, Rd, R, n, ptype):
+    from pysa_gb300 import unpack_spins
+    sp = unpack_spins(got["spins"].reshape(Rd, R, -1), n, ptype, np.float32)
+    bs = unpack_spins(got["best_spins"].reshape(Rd, R, -1), n, ptype,
+                      np.float32)
+    assert (sp == want["spins"]).all(), "spins"
+    assert (got["energies"].reshape(Rd, R) == want["energies"]).all()
+    assert (got["beta_idx"].reshape(Rd, R) == want["beta_idx"]).all()
+    assert (got["best_energy"].reshape(Rd, R) == want["best_energy"]).all()
+    assert (got["best_sweep"].reshape(Rd, R) == want["best_sweep"]).all()
+    assert (bs == want["best_spins"]).all(), "best spins"
+
+
+def _fused_batch(ptype, J, h, betas, Rd, fold):
+    from pysa_gb300 import Instance, PTBatch
+    b = PTBatch(ptype, [Instance(J, h, betas, Rd)], kernel="tc")
+    # the path under test: every instance on the tensor cores at this fold,
+    # exchange fused into the kernel
+    v = {1: 0, 2: 1, 4: 2}[fold]
+    assert b.tc and b.tc_terms == 1
+    assert b.ws.tc_variant_count[v] > 0
+    assert sum(b.ws.tc_variant_count[k] for k in range(3)) == \
+        b.ws.tc_variant_count[v]
+    assert b.ws.tc_fusable == 1 and b.ws.plain_live == 0
+    return b
+
+
+def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
+                   fold, graph_chunk=128):
+    """plan: the sweep counts of consecutive run() calls on one batch (each
+    call continues the previous one's chains, as Solver resumes)."""
+    from pysa_gb300 import pack_spins
+    rng = np.random.default_rng(seed)
+    J, h = _qubo(rng, n) if ptype == "qubo" else _ising_pm1(rng, n)
+    betas = (1.0 / np.geomspace(tmin, tmax, R)).astype(np.float32)
+    if ptype == "qubo":
+        x0 = rng.integers(0, 2, (Rd, R, n)).astype(np.float32)
+    else:
+        x0 = (2 * rng.integers(0, 2, (Rd, R, n)) - 1).astype(np.float32)
+    e0 = np.array([[oracle.energy64(J, h, s) for s in r] for r in x0],
+                  np.float32)
+    b = _fused_batch(ptype, J, h, betas, Rd, fold)
+    b.set_states(pack_spins(x0, ptype, b.words), e0)
+    bidx = np.tile(np.arange(R, dtype=np.int32), (Rd, 1))
+    state = (x0, e0, bidx, None)
+    done = 0
+    for sweeps in plan:
+        b.run(sweeps, seed=seed, graph_chunk=graph_chunk)
+        got = b.fetch()
+        sp, en, bi, best = state
+        want = oracle.pt_run(ptype, J, h, betas, sp, en, bi, seed=seed,
+                             num_sweeps=sweeps, first_sweep=done, best=best)
+        _check_equal(got, want, Rd, R, n, ptype)
+        state = (want["spins"], want["energies"], want["beta_idx"],
+                 (want["best_energy"], want["best_sweep"],
+                  want["best_spins"]))
+        done += sweeps
+    assert int(b.sweep_counter.item()) == done
+
+
+@pytest.mark.parametrize("plan", [(136,), (20,), (20, 13, 1)])
+def test_headline_qubo1024_fold2_fused_bit_exact(oracle, plan):
+    """136 sweeps: a 128-sweep launch of sixteen 8-sweep units, then one
+    8-sweep launch.  20 and 20 + 13 + 1: runs whose length is not a multiple
+    of the unit, resumed across calls."""
+    _run_vs_oracle(oracle, "qubo", 1024, 64, 3, 0.5, 8.0, plan, seed=11,
+                   fold=2)
+
+
+def test_headline_qubo1024_fold2_graph_replay_bit_exact(oracle):
+    """300 sweeps as run() issues them for long runs: two replays of a
+    captured 128-sweep graph, then 44 sweeps issued directly."""
+    _run_vs_oracle(oracle, "qubo", 1024, 64, 2, 0.5, 8.0, (300,), seed=12,
+                   fold=2)
+
+
+def test_headline_ising_pm1_fold2_fused_bit_exact(oracle):
+    _run_vs_oracle(oracle, "ising", 1000, 64, 2, 0.3, 3.0, (136,), seed=13,
+                   fold=2)
+
+
+@pytest.mark.parametrize("plan", [(136,), (20,)])
+def test_fold4_qubo1300_fused_bit_exact(oracle, plan):
+    _run_vs_oracle(oracle, "qubo", 1300, 32, 3, 0.5, 8.0, plan, seed=14,
+                   fold=4)
+
+
+def test_fold1_qubo512_fused_bit_exact(oracle):
+    _run_vs_oracle(oracle, "qubo", 512, 32, 4, 0.5, 8.0, (136,), seed=15,
+                   fold=1)

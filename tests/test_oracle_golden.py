@@ -82,3 +82,23 @@ def test_logz_exact_small(oracle):
         E = np.einsum("si,ij,sj->s", grid, J.astype(np.float64), grid) / 2 + grid @ h
         want = np.log(np.sum(np.exp(-0.7 * E)))
         assert abs(oracle.logz_exact(ptype, J, h, 0.7) - want) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["pt_ising_f64_seq", "pt_ising_f64_rand",
+                                  "pt_qubo_f64_seq"])
+def test_pt_f64_trajectory_matches_reference(oracle, name):
+    """The oracle's f64 driver (float_type='float64' arithmetic) against the
+    reference's update_spin run on f64 arrays with real couplings
+    (tests/golden/make_golden_f64.py): same decisions, energies to 1e-12
+    relative (the two f64 dots sum in different orders)."""
+    g = golden(name)
+    reads, R, _ = g["init_spins"].shape
+    out = oracle.pt_run64(str(g["problem_type"]), g["J"], g["h"], g["betas"],
+                          g["init_spins"], g["init_energies"],
+                          np.tile(np.arange(R, dtype=np.int32), (reads, 1)),
+                          seed=int(g["seed"]), num_sweeps=int(g["sweeps"]),
+                          update=str(g["update"]))
+    assert (out["spins"] == g["spins"]).all()
+    assert (out["beta_idx"] == g["beta_idx"]).all()
+    np.testing.assert_allclose(out["energies"], g["energies"], rtol=1e-12,
+                               atol=1e-12)
