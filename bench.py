@@ -1200,10 +1200,11 @@ def main():
                        "reads": Rd, "chains": C, "update": w["update"],
                        "exchange": "every sweep", "problem": w["kind"],
                        "l2": ("flushed (256 MB write) before every timed "
-                              "call of %d sweeps; fields stay in tensor "
-                              "memory within a launch" % chunk) if fused else
+                              "call of up to %d sweeps; fields stay in "
+                              "tensor memory within a launch" % chunk)
+                             if fused else
                              "flushed (256 MB write) before every step",
-                       "sweeps_per_launch": chunk,
+                       "sweeps_per_call": iters,
                        "kernel_choice": args.kernel,
                        "tc_min_n": batch.tc_min_n,
                        "kernel": ("persistent tensor-core blocked sweep "
