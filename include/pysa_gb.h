@@ -59,8 +59,11 @@ enum {
                                max(1, |E|), or is not finite */
 };
 
-/* Largest number of spins per instance the sweep kernels accept. */
-#define PYSA_GB_MAX_N 4096
+/* Largest number of spins per instance the sweep kernels accept.  Dense
+ * instances up to 4096 spins keep their fields in registers (plain kernel);
+ * wider ones keep them in the workspace's fields array (wide-instance
+ * kernel); 64 <= n <= 2048 can take the tensor cores. */
+#define PYSA_GB_MAX_N 65536
 
 /* A batch of dense problems (one or many instances, uneven sizes allowed). */
 typedef struct {
@@ -187,6 +190,12 @@ typedef struct {
   int32_t csr_width;
   int32_t csr_chains;     /* host, from pysa_gb_setup: chains per work item
                              (128, or 64 / 32 while that leaves SMs idle) */
+  /* host, from pysa_gb_setup: work items of the wide-instance sweep (dense
+   * instances with n > 4096: fields in this workspace's fields array, J
+   * read in place, so j_off and ld of those instances must be multiples
+   * of 4 and J 16-byte aligned) within items, 8 chains each */
+  int32_t wide_item_start;
+  int32_t wide_item_count;
   int32_t pad_;
 } pysa_gb_workspace;
 
@@ -299,8 +308,9 @@ int pysa_gb_sweeps(const pysa_gb_problems *p, pysa_gb_state *s,
  * resolves the array's address and should come before any stream capture;
  * the address stays cached, so after cudaDeviceReset the entry point must
  * not be called again on that device.  Dense couplings only: a batch with a
- * sparse-row instance (host->sparse) is rejected with PYSA_GB_ERR_ARG
- * before anything is enqueued.  Sequential and random order; never the
+ * sparse-row instance (host->sparse) is rejected with PYSA_GB_ERR_ARG, one
+ * with more than 4096 spins in an instance with PYSA_GB_ERR_SIZE, before
+ * anything is enqueued.  Sequential and random order; never the
  * tensor-core kernel. */
 int pysa_gb_sweeps_noalloc(const pysa_gb_problems *p, pysa_gb_state *s,
                            const pysa_gb_host_tables *host,

@@ -53,7 +53,8 @@ class Workspace(ctypes.Structure):
                 ("tc_diag_rand", P), ("tc_inst_off", P),
                 ("tc_rand_slots", I32), ("csr_item_start", I32),
                 ("csr_item_count", I32), ("csr_width", I32),
-                ("csr_chains", I32), ("pad_", I32)]
+                ("csr_chains", I32), ("wide_item_start", I32),
+                ("wide_item_count", I32), ("pad_", I32)]
 
 
 class HostTables(ctypes.Structure):

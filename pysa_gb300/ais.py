@@ -37,7 +37,8 @@ def omegas_to_partition(log_omegas, logZ0: float) -> float:
     lw = np.asarray(log_omegas, dtype=np.float64)
     smax = lw.max()
     expsum = np.sum(np.exp(lw - smax))
-    return float(smax - np.log(len(lw)) + logZ0 + np.log(expsum))
+    # np.float64, the type the reference returns (a frame's log_Zf column)
+    return np.float64(smax - np.log(len(lw)) + logZ0 + np.log(expsum))
 
 
 def combine_logZf(solution) -> float:
@@ -46,8 +47,8 @@ def combine_logZf(solution) -> float:
     log_Zf = np.asarray(col.to_numpy() if hasattr(col, "to_numpy") else col,
                         dtype=np.float64)
     smax = log_Zf.max()
-    return float(smax - np.log(len(log_Zf)) + np.log(np.sum(np.exp(log_Zf -
-                                                                    smax))))
+    return np.float64(smax - np.log(len(log_Zf)) +
+                      np.log(np.sum(np.exp(log_Zf - smax))))
 
 
 def partition_function_post(solution) -> float:

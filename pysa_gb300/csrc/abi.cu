@@ -9,6 +9,7 @@
 #include "ais_api.h"
 #include "csr_api.h"
 #include "tc_api.h"
+#include "wide_api.h"
 #include "aux.cuh"
 #include "plain_variants.h"
 #include "sweep_plain.cuh"
@@ -168,6 +169,12 @@ int pysa_gb_workspace_bytes(int32_t num_instances,
       if (nc > max_nc) max_nc = nc;
       continue;
     }
+    if (n > kPlainMaxN) {  // wide-instance sweep: J read in place
+      items += (chains + kWideWarps - 1) / kWideWarps;
+      const int nc = (n + 31) / 32;
+      if (nc > max_nc) max_nc = nc;
+      continue;
+    }
     const int v = plain_variant_for(n);
     const PlainVariant& pv = plain_variant(v);
     packed += (int64_t)n * row_floats(v);
@@ -207,9 +214,12 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   items.reserve(items_n);
   std::vector<int64_t> poff(p->num_instances);
   int64_t off = 0;
+  auto is_wide = [&](int i) {
+    return !is_sparse(host, i) && n_host[i] > kPlainMaxN;
+  };
   for (int i = 0; i < p->num_instances; ++i) {
     poff[i] = off;
-    if (!is_sparse(host, i))
+    if (!is_sparse(host, i) && !is_wide(i))
       off += (int64_t)n_host[i] * row_floats(plain_variant_for(n_host[i]));
   }
   for (int v = 0; v < kNumPlainVariants; ++v) {
@@ -267,6 +277,30 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     }
   }
   ws->csr_item_count = (int32_t)items.size() - ws->csr_item_start;
+  // wide dense instances: kWideWarps chains per item; J is read in place
+  // with 16-byte loads
+  ws->wide_item_start = (int32_t)items.size();
+  for (int i = 0; i < p->num_instances; ++i) {
+    if (!is_wide(i)) continue;
+    if (host->j_off[i] % 4 != 0 || host->ld[i] % 4 != 0 ||
+        reinterpret_cast<uintptr_t>(p->J) % 16 != 0)
+      return fail(PYSA_GB_ERR_ARG,
+                  "instances with n > 4096 need j_off and ld multiples of 4 "
+                  "and J 16-byte aligned");
+    const int64_t chains = (int64_t)replicas_host[i] * reads_host[i];
+    for (int64_t c = 0; c < chains; c += kWideWarps) {
+      SweepItem it;
+      it.inst = i;
+      it.chain0 = (int32_t)(chain_off_host[i] + c);
+      it.nchains = (int32_t)((chains - c) < kWideWarps ? (chains - c)
+                                                       : kWideWarps);
+      it.variant = -2;
+      it.poff_lo = it.poff_hi = 0;
+      it.pad0 = it.pad1 = 0;
+      items.push_back(it);
+    }
+  }
+  ws->wide_item_count = (int32_t)items.size() - ws->wide_item_start;
   if (!items.empty()) {
     cudaError_t e = cudaMemcpyAsync(ws->items, items.data(),
                                     items.size() * sizeof(SweepItem),
@@ -277,7 +311,7 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   for (int i = 0; i < p->num_instances; ++i) {
     if (host->ld[i] < n_host[i])
       return fail(PYSA_GB_ERR_ARG, "ld < n");
-    if (is_sparse(host, i)) continue;
+    if (is_sparse(host, i) || is_wide(i)) continue;
     const int v = plain_variant_for(n_host[i]);
     launch_pack_rows(p->J + host->j_off[i], host->ld[i], n_host[i],
                      plain_variant(v).nc, lane_stride(v),
@@ -377,7 +411,8 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     boff[i] = bo;
     doff[i] = dd;
     if (!tc_selected(host, i, min_n)) {
-      if (!is_sparse(host, i)) live |= 1 << plan.variant_of(host->n[i]);
+      if (!is_sparse(host, i) && host->n[i] <= kPlainMaxN)
+        live |= 1 << plan.variant_of(host->n[i]);
       continue;
     }
     if (tc_chains_per_cta(host->n[i]) % host->replicas[i] != 0) fusable = 0;
@@ -603,7 +638,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   // (or none), no log-omega; several sweeps per launch with the fields
   // resident in tensor memory.
   const bool fused = use_tc && phases == 3 && ws->plain_live == 0 &&
-                     ws->csr_item_count == 0 &&
+                     ws->csr_item_count == 0 && ws->wide_item_count == 0 &&
                      o->log_omega_stride == 0 &&
                      (!o->use_pt || ws->tc_fusable) && ws->tc_sched;
   // random order on the tensor cores: visiting orders of the next `cnt`
@@ -677,6 +712,23 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
       ca.chains = ws->csr_chains > 0 ? ws->csr_chains : kCsrChains;
       cudaError_t e = launch_csr(ca, random, st);
       if (e != cudaSuccess) return cuda_fail(e, "sparse sweep launch");
+    }
+    if ((phases & 1) && ws->wide_item_count > 0) {
+      // (random order: the visiting order was made in the loop above)
+      WideArgs wa;
+      wa.p = *p;
+      wa.s = *s;
+      wa.perm = ws->perm;
+      wa.fields = ws->fields;
+      wa.field_ld = ws->field_ld;
+      wa.perm_slots = a.perm_slots;
+      wa.items = reinterpret_cast<const SweepItem*>(ws->items) +
+                 ws->wide_item_start;
+      wa.num_items = ws->wide_item_count;
+      wa.pad_ = 0;
+      wa.seed = o->seed;
+      cudaError_t e = launch_wide(wa, random, 4 * sms, st);
+      if (e != cudaSuccess) return cuda_fail(e, "wide sweep launch");
     }
     if (phases & 2) launch_exchange(x, st);
   }

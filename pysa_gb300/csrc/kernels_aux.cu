@@ -245,10 +245,53 @@ __global__ void k_perm(const PermArgs a) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = p[i];
 }
 
+// The same orders for instances too wide for k_perm's shared memory (up to
+// 65536 spins): the draws are staged in the output row, the positions held
+// as 16-bit values in shared memory.
+__global__ void k_perm_wide(const PermArgs a) {
+  extern __shared__ uint16_t pw[];
+  const int inst = blockIdx.x;
+  const int n = a.p.n[inst];
+  const uint32_t sweep = (uint32_t)(*a.sweep_counter) + blockIdx.y;
+  int32_t* out = a.perm + ((int64_t)(sweep % (uint32_t)a.perm_slots) *
+                               a.p.num_instances + inst) * (int64_t)a.p.max_n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    pw[i] = (uint16_t)i;
+    out[i] = (int32_t)draw1(a.seed, TAG_PERM, (uint32_t)inst, sweep, 0u,
+                            (uint32_t)i);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = n - 1; i > 0; --i) {
+      const uint32_t xi = (uint32_t)__ldcg(out + i);
+      const int j = (int)(((uint64_t)xi * (uint64_t)(i + 1)) >> 32);
+      const uint16_t t = pw[i];
+      pw[i] = pw[j];
+      pw[j] = t;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = (int32_t)pw[i];
+}
+
 void launch_perm(const PermArgs& a, cudaStream_t st, int count) {
   const size_t sm = sizeof(int32_t) * 2 * (size_t)a.p.max_n;
   dim3 grid((unsigned)a.p.num_instances, (unsigned)(count > 0 ? count : 1));
-  k_perm<<<grid, 256, sm, st>>>(a);
+  if (sm <= 48 * 1024) {
+    k_perm<<<grid, 256, sm, st>>>(a);
+    return;
+  }
+  const size_t smw = sizeof(uint16_t) * (size_t)a.p.max_n;  // <= 128 KB
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    cudaFuncSetAttribute(k_perm_wide,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(uint16_t) * PYSA_GB_MAX_N));
+    attr[dev] = true;
+  }
+  k_perm_wide<<<grid, 256, smw, st>>>(a);
 }
 
 // ----------------------------------------------------------- f64 energy

@@ -22,8 +22,10 @@
 //     process: cudaDeviceReset (or anything else that re-creates the
 //     device's primary context) leaves it stale, so do not call this entry
 //     point again on a device after resetting it.
-//   * Dense couplings only: a batch with a sparse-row instance
-//     (pysa_gb_host_tables.sparse) is rejected before anything is enqueued.
+//   * Dense couplings of at most 4096 spins per instance (the
+//     register-resident plain kernel): a batch with a sparse-row instance
+//     (pysa_gb_host_tables.sparse) or a wider one is rejected before
+//     anything is enqueued.
 //   * It allocates nothing: no cudaMalloc / cudaFree, no host heap.  The
 //     work list is rebuilt on the device on every call by one CTA in
 //     O(instances / 256 + log 256) steps.
@@ -32,6 +34,7 @@
 #include "aux.cuh"
 #include "plain_variants.h"
 #include "sweep_plain.cuh"
+#include "wide_api.h"
 
 namespace pysa_gb {
 
@@ -150,6 +153,13 @@ extern "C" int pysa_gb_sweeps_noalloc(const pysa_gb_problems* p,
             PYSA_GB_ERR_ARG,
             "sweeps_noalloc: sparse-row instances are not supported (dense "
             "couplings only); use pysa_gb_sweeps with a workspace");
+  // the register-resident plain kernel only (n <= 4096)
+  for (int i = 0; i < p->num_instances; ++i)
+    if (host->n[i] > kPlainMaxN)
+      return pysa_gb_internal_fail(
+          PYSA_GB_ERR_SIZE,
+          "sweeps_noalloc: instances with more than 4096 spins are not "
+          "supported; use pysa_gb_sweeps with a workspace");
   int64_t need[3];
   const int items_n = pysa_gb_workspace_bytes(p->num_instances, host, need);
   if (items_n < 0) return items_n;

@@ -52,7 +52,7 @@ def test_workspace_plan_host_only():
     assert out[1] == items * 8
 
 
-@pytest.mark.parametrize("bad", [([0], [4], [1]), ([5000], [4], [1]),
+@pytest.mark.parametrize("bad", [([0], [4], [1]), ([70000], [4], [1]),
                                  ([10], [0], [1]), ([10], [600], [1])])
 def test_workspace_rejects_bad_sizes(bad):
     from pysa_gb300 import _lib
@@ -61,6 +61,19 @@ def test_workspace_rejects_bad_sizes(bad):
     out = (ctypes.c_int64 * 3)()
     assert lib.pysa_gb_workspace_bytes(1, ctypes.byref(ht), out) < 0
     assert lib.pysa_gb_last_error()
+
+
+def test_workspace_plan_wide_instances():
+    """Dense instances above 4096 spins take the wide-instance sweep: eight
+    chains per work item, no packed couplings, fields as wide as n."""
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    arrs, ht = _tables([6000, 100, 65536], [5, 8, 2], [3, 2, 1])
+    out = (ctypes.c_int64 * 3)()
+    items = lib.pysa_gb_workspace_bytes(3, ctypes.byref(ht), out)
+    assert items == 2 + 1 + 1          # 15 / 8, 16 / 64, 2 / 8
+    assert out[0] == 100 * 32 * 4       # packed rows of the n = 100 instance
+    assert out[2] == 65536
 
 
 def test_null_arguments_rejected_without_gpu():
