@@ -52,9 +52,10 @@ WORKLOADS = {
                              reads=100, tmin=1.0, tmax=3.5),
     "rbm_mnist": dict(kind="rbm", visible=784, hidden=128, state_size=100,
                       steps=1, tmin=1.0, tmax=1.0, parallel=False),
-    "sk512_tts": dict(kind="pm1", n=512, replicas=64, reads=128, tmin=0.3,
-                      tmax=3.0, instances=64, budgets=(1000, 4000, 16000),
-                      target_sweeps=32000, update="sequential"),
+    "sk512_tts": dict(kind="pm1", n=512, replicas=64, reads=32, tmin=0.3,
+                      tmax=3.0, instances=64, budgets=(25000, 100000),
+                      target_sweeps=100000, target_reads=4, plain_check=200,
+                      target_flips=2.0, update="sequential"),
 }
 
 
@@ -275,23 +276,48 @@ def cpu_reference(w, ptype, P, reads, sweeps, nthreads=0):
     return reads * R * n * sweeps / dt, dt
 
 
-def run_tts_workload(args, w, rank, world):
-    """TTS(99%) of plain GPU PT against PT with the learned proposal on
-    seeded +-1 SK instances (J_ij = +-1 symmetric, zero diagonal).
+def _median_tts_boot(success, t_run, rng, nboot=400, ptgt=0.99):
+    """Bootstrap of the median over instances of TTS(ptgt): each instance's
+    reads resampled with replacement (as tests/test_tts.py:257-277 does for
+    its quantile).  success [I, Rd] bool; t_run seconds per read."""
+    from pysa_gb300.tts import nts
+    I, Rd = success.shape
+    out = np.empty(nboot)
+    for b in range(nboot):
+        idx = rng.integers(0, Rd, (I, Rd))
+        t = nts(np.take_along_axis(success, idx, axis=1), ptgt) * t_run
+        out[b] = np.median(t)
+    return out
 
-    Target energy of each instance: the lowest energy seen by a long plain
-    run (target_sweeps) or by any arm.  Each arm restarts from the same
-    random states for every sweep budget S; one run = one read, all
-    I x Rd reads run concurrently, so t_run = wall time / (I Rd) and
-    TTS = t_run ln(0.01) / ln(1 - p_s) (per instance; the line reports the
-    median over instances at the best budget).  The learned arm's wall time
-    includes its online training and proposals."""
+
+def run_tts_workload(args, w, rank, world):
+    """TTS(99 %) on seeded +-1 SK instances (J_ij = +-1 symmetric, zero
+    diagonal), three arms:
+
+      plain          the plain CUDA-core PT sweep (k_sweep_plain)
+      split_bf16     the blocked split-BF16 tensor-core PT sweep (k_sweep_tc)
+      learned        split_bf16 plus the learned flip proposal
+
+    Target energy per instance: the best energy of a target_sweeps plain PT
+    run (target_reads reads, its own seed).  Each arm runs every budget S
+    from the same random states; one run = one read, all I x Rd reads run
+    concurrently, so t_run = wall time / (I Rd) and TTS = t_run ln(0.01) /
+    ln(1 - p_s), p_s = fraction of reads whose best reaches the target.
+    +-1 couplings are exact in BF16, so the tensor-core sweep's trajectories
+    equal the plain kernel's bit for bit on the same stream: the plain arm
+    is run for plain_check sweeps, its chains compared with the split_bf16
+    arm's after as many sweeps (must be identical), its wall time per sweep
+    measured there, and its TTS at budget S formed from that time and the
+    split_bf16 arm's success rates.  The target run uses the tensor-core
+    sweep for the same reason.  CIs: bootstrap of the median TTS over
+    instances (reads resampled per instance), and of the ratio of two arms'
+    medians; the learned arm's time includes its training and proposals."""
     if rank != 0:
         return 0
     import torch
     from pysa_gb300 import Instance, PTBatch, pack_spins
     from pysa_gb300.proposal import LearnedProposal, run_with_proposals
-    from pysa_gb300.tts import batch_tts
+    from pysa_gb300.tts import nts
     I, n, R, Rd = w["instances"], w["n"], w["replicas"], w["reads"]
     rng = np.random.default_rng(2024)
     Js = []
@@ -300,97 +326,134 @@ def run_tts_workload(args, w, rank, world):
         Js.append((J + J.T).astype(np.float32))
     h0 = np.zeros(n, np.float32)
     lad = np.sort(ladder(w)).astype(np.float32)
-    x0 = (2 * np.random.default_rng(7).integers(0, 2, (I * Rd * R, n)) - 1
-          ).astype(np.float32)
 
-    def fresh():
-        b = PTBatch("ising", [Instance(J, h0, lad, Rd) for J in Js])
+    def fresh(reads, kernel="tc", seed_states=7):
+        x0 = (2 * np.random.default_rng(seed_states).integers(
+            0, 2, (I * reads * R, n)) - 1).astype(np.float32)
+        b = PTBatch("ising", [Instance(J, h0, lad, reads) for J in Js],
+                    kernel=kernel)
         b.set_states(pack_spins(x0, "ising", b.words))
         torch.cuda.synchronize()
         return b
 
-    def per_read_best(b):
-        return b.best_energy.view(I, Rd, R).min(dim=2).values.cpu().numpy()
+    def per_read_best(b, reads):
+        return b.best_energy.view(I, reads, R).min(dim=2).values.cpu().numpy()
 
     sampler = ClockSampler(0)
     with sampler:
-        b = fresh()
+        # target: best of a target_sweeps run
+        b = fresh(w["target_reads"], seed_states=8)
         t0 = time.perf_counter()
         b.run(w["target_sweeps"], seed=11)
         torch.cuda.synchronize()
         t_target = time.perf_counter() - t0
         b.check_status()
-        target = per_read_best(b).min(axis=1)
+        target = per_read_best(b, w["target_reads"]).min(axis=1)
         del b
-        arms = {"plain": {}, "learned": {}}
+        # plain arm: identical trajectories to split_bf16, timed per sweep
+        K = w["plain_check"]
+        bp = fresh(Rd, kernel="plain")
+        bp.run(1, seed=13)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bp.run(K - 1, seed=13)
+        torch.cuda.synchronize()
+        t_plain_sweep = (time.perf_counter() - t0) / (K - 1)
+        bs_ = fresh(Rd)
+        bs_.run(K, seed=13)
+        torch.cuda.synchronize()
+        same = bool(torch.equal(bp.spins, bs_.spins) and
+                    torch.equal(bp.best_energy, bs_.best_energy) and
+                    torch.equal(bp.beta_idx, bs_.beta_idx))
+        if not same:
+            raise AssertionError("plain and tensor-core sweeps diverged")
+        del bp, bs_
+        arms = {"split_bf16": {}, "learned": {}}
         stats = {}
         for S in w["budgets"]:
-            b = fresh()
+            b = fresh(Rd)
             t0 = time.perf_counter()
             b.run(S, seed=13)
             torch.cuda.synchronize()
-            arms["plain"][S] = (time.perf_counter() - t0, per_read_best(b))
+            arms["split_bf16"][S] = (time.perf_counter() - t0,
+                                     per_read_best(b, Rd))
             b.check_status()
             del b
-            b = fresh()
+            b = fresh(Rd)
             prop = LearnedProposal(b, hidden=1024, lr=1e-3, init_seed=3,
-                                   target_flips=2.0)
+                                   target_flips=w["target_flips"])
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             st = run_with_proposals(b, prop, S, seed=13, interval=10,
                                     train_every=5, train_pairs=200_000,
                                     min_train_steps=200, min_accept=0.01)
             torch.cuda.synchronize()
-            arms["learned"][S] = (time.perf_counter() - t0, per_read_best(b))
+            arms["learned"][S] = (time.perf_counter() - t0,
+                                  per_read_best(b, Rd))
             b.check_status()
-            pb = arms["plain"][S][1]
-            lb = arms["learned"][S][1]
             stats[S] = {"rounds": st.rounds, "train_steps": st.train_steps,
                         "acceptance_mean": float(st.acceptance.mean()),
                         "accepted_moves": int(st.accepted.sum()),
-                        "enabled_instances_at_end": int(st.enabled.sum()),
-                        "chains_moved_to_new_streams":
-                            int((b.stream_key != 0).sum().item()),
-                        "reads_best_lower_than_plain": int((lb < pb).sum()),
-                        "reads_best_higher_than_plain": int((lb > pb).sum())}
+                        "enabled_instances_at_end": int(st.enabled.sum())}
             del b, prop
-    for arm in arms.values():
-        for S, (_, best) in arm.items():
-            target = np.minimum(target, best.min(axis=1))
+    rb = np.random.default_rng(99)
+    tg = target[:, None] + 1e-6
     out = {}
-    per = {name: {S: batch_tts(best, target, t)["tts"]
-                  for S, (t, best) in arm.items()} for name, arm in arms.items()}
-    for name, arm in arms.items():
-        rows = {}
-        for S, (t, best) in arm.items():
-            r = batch_tts(best, target, t)
-            both = np.isfinite(per["plain"][S]) & np.isfinite(per["learned"][S])
-            geo = (float(np.exp(np.mean(np.log(r["tts"][both]))))
-                   if both.any() else None)
-            rows[S] = {"seconds": t, "tts_median_s": r["tts_median"],
-                       "p_success_mean": float(r["success_prob"].mean()),
-                       "solved_instances": r["solved_instances"],
-                       "tts_geomean_s_solved_by_both": geo,
-                       "instances_solved_by_both": int(both.sum())}
-        bestS = min(rows, key=lambda k: rows[k]["tts_median_s"])
-        out[name] = {"tts99_median_s": rows[bestS]["tts_median_s"],
-                     "best_budget_sweeps": bestS,
-                     "budgets": {str(k): v for k, v in rows.items()}}
+    boots = {}
+    for S in w["budgets"]:
+        t_split, best_split = arms["split_bf16"][S]
+        t_learn, best_learn = arms["learned"][S]
+        succ = {"split_bf16": best_split <= tg, "learned": best_learn <= tg}
+        succ["plain"] = succ["split_bf16"]   # identical trajectories
+        t_run = {"split_bf16": t_split / (I * Rd),
+                 "learned": t_learn / (I * Rd),
+                 "plain": t_plain_sweep * S / (I * Rd)}
+        row = {}
+        for arm in ("plain", "split_bf16", "learned"):
+            tts = nts(succ[arm]) * t_run[arm]
+            bt = _median_tts_boot(succ[arm], t_run[arm], rb)
+            boots[(arm, S)] = bt
+            fin = bt[np.isfinite(bt)]
+            row[arm] = {
+                "seconds": t_run[arm] * I * Rd,
+                "p_success_mean": float(succ[arm].mean()),
+                "instances_with_success": int(succ[arm].any(axis=1).sum()),
+                "tts99_median_s": float(np.median(tts)),
+                "tts99_median_ci95_s": ([float(np.quantile(bt, 0.025)),
+                                         float(np.quantile(bt, 0.975))]
+                                        if len(fin) == len(bt) else None)}
+        for a, b_ in (("plain", "learned"), ("split_bf16", "learned"),
+                      ("plain", "split_bf16")):
+            ra = boots[(a, S)] / boots[(b_, S)]
+            ok = np.isfinite(ra)
+            row[f"ratio_{a}_over_{b_}"] = {
+                "median": float(np.median(ra[ok])) if ok.any() else None,
+                "ci95": [float(np.quantile(ra[ok], 0.025)),
+                         float(np.quantile(ra[ok], 0.975))]
+                if ok.sum() == len(ra) else None}
+        out[str(S)] = row
+    bestS = min(w["budgets"],
+                key=lambda S: out[str(S)]["learned"]["tts99_median_s"])
     line = {
-        "metric": "tts99_median_s", "value": out["learned"]["tts99_median_s"],
+        "metric": "tts99_median_s",
+        "value": out[str(bestS)]["learned"]["tts99_median_s"],
         "unit": "s", "n_gpus": 1, "steps": len(w["budgets"]), "warmup": 0,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 sweeps; bf16/f32 network", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "instances": I, "n": n,
                    "replicas": R, "reads": Rd, "tmin": w["tmin"],
                    "tmax": w["tmax"], "budgets": list(w["budgets"]),
-                   "target_sweeps": w["target_sweeps"],
+                   "target": f"best of a {w['target_sweeps']}-sweep plain "
+                             f"PT run, {w['target_reads']} reads",
                    "target_seconds": t_target,
-                   "network": "512-1024-512 per instance, target 2 flips, "
-                              "propose every 10 sweeps, train every 5 "
-                              "(2e5 pairs max), off below 1% acceptance "
-                              "after 200 training steps"},
-        "learned": out["learned"], "plain_gpu": out["plain"],
+                   "plain_arm": f"same trajectories as split_bf16 (checked "
+                                f"over {K} sweeps), {t_plain_sweep * 1e3:.3f}"
+                                f" ms per sweep",
+                   "network": "512-1024-512 per instance, target "
+                              f"{w['target_flips']} flips, propose every "
+                              "10 sweeps, train every 5 (2e5 pairs max), off "
+                              "below 1% acceptance after 200 training steps"},
+        "best_budget_sweeps": bestS, "budgets": out,
         "proposal_stats": {str(k): v for k, v in stats.items()},
         "clocks": sampler.summary(),
     }

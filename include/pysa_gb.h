@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define PYSA_GB_ABI_VERSION 1
+#define PYSA_GB_ABI_VERSION 2
 
 enum {
   PYSA_GB_ISING = 0,
@@ -196,7 +196,13 @@ typedef struct {
    * of 4 and J 16-byte aligned) within items, 8 chains each */
   int32_t wide_item_start;
   int32_t wide_item_count;
-  int32_t pad_;
+  /* caller: chains per tensor-core work item (0: automatic -- a CTA's full
+   * tensor memory, 128 / F chains, halved while the batch would leave SMs
+   * idle); otherwise the largest multiple of each instance's granule (R
+   * when R divides 128 / F, else 32) not above min(this, 128 / F).  Read
+   * by pysa_gb_tc_setup; pysa_gb_tc_workspace sizes for the smallest
+   * items any value can give. */
+  int32_t tc_item_chains;
 } pysa_gb_workspace;
 
 /* Host copies of the per-instance tables, used to plan the work list. */
@@ -224,6 +230,13 @@ typedef struct {
   int32_t recompute_every; /* tensor-core sweep: rebuild fields and energies
                               from the spins at the start of every sweep whose
                               index is a multiple of this (0 = never) */
+  int32_t exchange_every;  /* 0 or 1: replica exchange after every sweep, as
+                              pysa/simulation.py:167-168 does; k > 1: only
+                              after sweeps s with (s + 1) % k == 0 (an opt-in
+                              tuning knob with no counterpart in the
+                              reference; log-omega is still taken every
+                              sweep) */
+  int32_t pad_;
 } pysa_gb_options;
 
 /* ABI version (PYSA_GB_ABI_VERSION) and the last error of this thread. */

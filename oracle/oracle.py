@@ -48,6 +48,7 @@ class _PtArgs(ctypes.Structure):
                 ("reads", ctypes.c_int32), ("inst", ctypes.c_int32),
                 ("update", ctypes.c_int32), ("use_pt", ctypes.c_int32),
                 ("best_mode", ctypes.c_int32), ("log_omega", ctypes.c_int32),
+                ("exchange_every", ctypes.c_int32),
                 ("seed", ctypes.c_uint64)]
 
 
@@ -172,7 +173,8 @@ def pt_run(problem_type: str,
            best: tuple | None = None,
            log_omega: bool = False,
            inst: int = 0,
-           nthreads: int = 0):
+           nthreads: int = 0,
+           exchange_every: int = 1):
     """Run the oracle PT driver in place-free form.
 
     spins: [reads, R, n] float32 (+-1 or 0/1); energies [reads, R] float32;
@@ -201,7 +203,7 @@ def pt_run(problem_type: str,
     args = _PtArgs(0 if problem_type == "ising" else 1, n, J.shape[1], R,
                    reads, inst, 1 if update == "random" else 0, int(use_pt),
                    0 if best_mode == "replica" else 1, int(log_omega),
-                   seed & ((1 << 64) - 1))
+                   int(exchange_every), seed & ((1 << 64) - 1))
     st = _PtState(sp.ctypes.data, en.ctypes.data, bi.ctypes.data,
                   be.ctypes.data, bs.ctypes.data, bsp.ctypes.data,
                   lo.ctypes.data, stride)
@@ -233,7 +235,8 @@ def pt_run64(problem_type: str,
              update: str = "sequential",
              use_pt: bool = True,
              inst: int = 0,
-             nthreads: int = 0):
+             nthreads: int = 0,
+             exchange_every: int = 1):
     """The PT driver in f64 throughout: the reference's arithmetic for a
     Solver built with float_type='float64' (pysa/sa.py:204-205).  Same
     stream and arguments as pt_run (per-replica best); arrays in f64."""
@@ -247,7 +250,7 @@ def pt_run64(problem_type: str,
     be, bs, bsp = en.copy(), np.zeros_like(bi), sp.copy()
     args = _PtArgs(0 if problem_type == "ising" else 1, n, J.shape[1], R,
                    reads, inst, 1 if update == "random" else 0, int(use_pt),
-                   0, 0, seed & ((1 << 64) - 1))
+                   0, 0, int(exchange_every), seed & ((1 << 64) - 1))
     st = _PtState64(sp.ctypes.data, en.ctypes.data, bi.ctypes.data,
                     be.ctypes.data, bs.ctypes.data, bsp.ctypes.data)
     rc = lib().orc_pt_run64(ctypes.byref(args), _p(J), _p(h), _p(betas),

@@ -164,8 +164,15 @@ typedef struct {
   int32_t use_pt;
   int32_t best_mode;    /* 0 per replica (simulation_parallel), 1 global */
   int32_t log_omega;    /* 1: record get_log_omega per sweep */
+  int32_t exchange_every; /* <= 1: exchange after every sweep (the
+                             reference); k: only after sweeps with
+                             (s + 1) % k == 0 (the GPU's opt-in knob) */
   uint64_t seed;
 } orc_pt_args;
+
+static inline int exchange_after(const orc_pt_args *a, int64_t sw) {
+  return a->exchange_every <= 1 || (sw + 1) % a->exchange_every == 0;
+}
 
 typedef struct {
   float *spins;       /* [reads*R, n] values +-1 or {0,1} */
@@ -266,7 +273,8 @@ int orc_pt_run(const orc_pt_args *a, const float *J, const float *h,
     for (int rd = 0; rd < Rd; ++rd) {
       int32_t *bidx = st->beta_idx + (int64_t)rd * R;
       const float *E = st->energies + (int64_t)rd * R;
-      if (a->use_pt) pt_step(a, betas, E, bidx, (uint32_t)rd, sweep);
+      if (a->use_pt && exchange_after(a, sw))
+        pt_step(a, betas, E, bidx, (uint32_t)rd, sweep);
       if (a->log_omega)
         st->log_omega[(int64_t)rd * st->lo_stride + sw] =
             log_omega_of(R, betas, sorted_slots, bidx, E);
@@ -357,7 +365,7 @@ int orc_pt_run64(const orc_pt_args *a, const double *J, const double *h,
         memcpy(st->best_spins + c * n, sp, sizeof(double) * (size_t)n);
       }
     }
-    if (!a->use_pt) continue;
+    if (!a->use_pt || !exchange_after(a, sw)) continue;
     for (int rd = 0; rd < Rd; ++rd) {
       int32_t *bidx = st->beta_idx + (int64_t)rd * R;
       const double *E = st->energies + (int64_t)rd * R;

@@ -54,7 +54,7 @@ class Workspace(ctypes.Structure):
                 ("tc_rand_slots", I32), ("csr_item_start", I32),
                 ("csr_item_count", I32), ("csr_width", I32),
                 ("csr_chains", I32), ("wide_item_start", I32),
-                ("wide_item_count", I32), ("pad_", I32)]
+                ("wide_item_count", I32), ("tc_item_chains", I32)]
 
 
 class HostTables(ctypes.Structure):
@@ -65,7 +65,8 @@ class HostTables(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("seed", U64), ("update", I32), ("use_pt", I32),
                 ("log_omega_stride", I32), ("best_global", I32),
-                ("phases", I32), ("recompute_every", I32)]
+                ("phases", I32), ("recompute_every", I32),
+                ("exchange_every", I32), ("pad_", I32)]
 
 
 class Mlp(ctypes.Structure):
@@ -142,7 +143,7 @@ def load() -> ctypes.CDLL:
         f = getattr(lib, name)
         f.argtypes = args
         f.restype = res
-    if lib.pysa_gb_abi_version() != 1:
+    if lib.pysa_gb_abi_version() != 2:
         raise LibraryError("libpysa_gb ABI version mismatch")
     _lib = lib
     return lib

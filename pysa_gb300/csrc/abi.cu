@@ -328,20 +328,31 @@ static inline bool tc_selected(const pysa_gb_host_tables* host, int i,
   return !is_sparse(host, i) && n >= (min_n < 64 ? 64 : min_n) && n <= 2048;
 }
 
-// Chains per tensor-core work item of every selected instance: a CTA's full
-// tensor memory (128/F chains), halved while the batch would fill fewer
-// CTAs than the GPU has SMs and the halves still hold whole reads (or whole
-// warps when R does not divide 128/F).  0 for instances left to the plain
-// kernel.
+// Chains per tensor-core work item of every selected instance.  fixed = 0:
+// a CTA's full tensor memory (128/F chains), halved while the batch would
+// fill fewer CTAs than the GPU has SMs and the halves still hold whole reads
+// (or whole warps when R does not divide 128/F).  fixed > 0: the largest
+// multiple of the instance's granule (R, or 32) not above min(fixed, 128/F),
+// at least one granule.  fixed < 0: one granule (the smallest items, for
+// sizing).  0 for instances left to the plain kernel.
 static std::vector<int> tc_item_sizes(int num_instances,
                                       const pysa_gb_host_tables* host,
-                                      int min_n) {
+                                      int min_n, int fixed) {
   std::vector<int> size(num_instances, 0), gran(num_instances, 32);
   for (int i = 0; i < num_instances; ++i) {
     if (!tc_selected(host, i, min_n)) continue;
     size[i] = tc_chains_per_cta(host->n[i]);
     if (size[i] % host->replicas[i] == 0) gran[i] = host->replicas[i];
+    if (gran[i] > size[i]) gran[i] = size[i];
+    if (fixed < 0) {
+      size[i] = gran[i];
+    } else if (fixed > 0) {
+      const int cap = fixed < size[i] ? fixed : size[i];
+      const int m = cap / gran[i] * gran[i];
+      size[i] = m > 0 ? m : gran[i];
+    }
   }
+  if (fixed != 0) return size;
   const int sms = sm_count();
   for (;;) {
     int64_t items = 0;
@@ -372,7 +383,8 @@ int pysa_gb_tc_workspace(int32_t num_instances,
   for (int i = 0; i < num_instances; ++i)
     if (host->replicas[i] < 1 || host->reads[i] < 0)
       return fail(PYSA_GB_ERR_ARG, "tc_workspace: bad replicas or reads");
-  const std::vector<int> isz = tc_item_sizes(num_instances, host, min_n);
+  // capacity for the smallest items tc_item_chains can ask for
+  const std::vector<int> isz = tc_item_sizes(num_instances, host, min_n, -1);
   int64_t b = 0, d = 0, items = 0;
   for (int i = 0; i < num_instances; ++i) {
     const int n = host->n[i];
@@ -421,7 +433,10 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     dd += tc_diag_elems(host->n[i]);
   }
   std::vector<TcItem> items;
-  const std::vector<int> isz = tc_item_sizes(p->num_instances, host, min_n);
+  if (ws->tc_item_chains < 0)
+    return fail(PYSA_GB_ERR_ARG, "tc_item_chains must be >= 0");
+  const std::vector<int> isz =
+      tc_item_sizes(p->num_instances, host, min_n, ws->tc_item_chains);
   const int folds[3] = {1, 2, 4};
   for (int v = 0; v < 3; ++v) {
     ws->tc_variant_start[v] = (int32_t)items.size();
@@ -578,6 +593,8 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   x.seed = o->seed;
   x.use_pt = o->use_pt;
   x.log_omega_stride = o->log_omega_stride;
+  x.exchange_every = o->exchange_every;
+  x.pad_ = 0;
   PermArgs pa;
   pa.p = *p;
   pa.sweep_counter = s->sweep_counter;
@@ -597,7 +614,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.seed = o->seed;
   ta.recompute_every = o->recompute_every;
   ta.use_pt = o->use_pt;
-  ta.pad_ = 0;
+  ta.exchange_every = o->exchange_every;
   ta.unit_wait_ns = g_unit_wait_ns;
   ta.sched = ws->tc_sched;
   ta.perm = ws->perm;

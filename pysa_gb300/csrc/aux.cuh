@@ -23,7 +23,14 @@ struct XArgs {
   uint64_t seed;
   int32_t use_pt;
   int32_t log_omega_stride;
+  int32_t exchange_every;  // <= 1: every sweep; k: after sweeps (s+1) % k == 0
+  int32_t pad_;
 };
+
+// Whether sweep `sweep` ends with a replica exchange.
+__host__ __device__ inline bool exchange_after(int32_t every, uint32_t sweep) {
+  return every <= 1 || (sweep + 1u) % (uint32_t)every == 0u;
+}
 
 struct PermArgs {
   pysa_gb_problems p;

@@ -150,6 +150,7 @@ __global__ void k_exchange(const XArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t r = (int64_t)blockIdx.x * kXWarps + warp;
   const uint32_t sweep = (uint32_t)(*a.s.sweep_counter);
+  const bool xch = a.use_pt && exchange_after(a.exchange_every, sweep);
   if (r < a.p.num_reads) {
     const int inst = a.p.read_inst[r];
     const int R = a.p.replicas[inst];
@@ -162,12 +163,12 @@ __global__ void k_exchange(const XArgs a) {
     for (int k = lane; k < R; k += 32) {
       E[k] = a.s.energies[base + k];
       B[k] = a.s.beta_idx[base + k];
-      if (a.use_pt && k < R - 1)
+      if (xch && k < R - 1)
         X[k] = draw1(a.seed, TAG_PT, (uint32_t)inst, sweep, (uint32_t)lread,
                      (uint32_t)k);
     }
     __syncwarp();
-    if (a.use_pt && R > 1 && lane == 0) {
+    if (xch && R > 1 && lane == 0) {
       for (int k = 0; k < R - 1; ++k) {
         const int k1 = R - k - 1, k2 = R - k - 2;
         const int b1 = B[k1], b2 = B[k2];

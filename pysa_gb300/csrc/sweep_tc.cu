@@ -1081,7 +1081,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           ex_E[c] = e_f;
         }
         named_sync_128();
-        if (a.fuse_exchange && a.use_pt && !*sh.abort) {
+        if (a.fuse_exchange && a.use_pt &&
+            exchange_after(a.exchange_every, sweep) && !*sh.abort) {
           // pysa/utils.py:44-58 per read, warp per read: pairs (R-1, R-2),
           // (R-2, R-3), ... in order; uniforms of stream (PT, inst, sweep,
           // read, pair)

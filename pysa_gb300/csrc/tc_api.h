@@ -31,7 +31,7 @@ struct TcArgs {
   int32_t fuse_exchange;    // 1: exchange inside the kernel (R | chains/CTA)
   int32_t use_pt;
   int32_t advance_counter;  // 1: the last CTA advances the sweep counter
-  int32_t pad_;
+  int32_t exchange_every;   // <= 1: every sweep; k: after (s + 1) % k == 0
   uint64_t unit_wait_ns;  // bound of the wait for an item's previous unit
                           // (0: one second)
   int32_t* sched;  // zeroed per launch: [0] unit queue, [1] finished CTAs,

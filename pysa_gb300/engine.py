@@ -305,9 +305,11 @@ class PTBatch:
             raise ValueError(f"unknown kernel {kernel!r}")
         self.autotune_pending = kernel == "autotune"
 
-    def _setup_tc(self, min_n: int | None):
+    def _setup_tc(self, min_n: int | None, item_chains: int | None = None):
         """Select the tensor-core sweep for instances with
-        min_n <= n <= 2048 (None: plain kernel for every instance)."""
+        min_n <= n <= 2048 (None: plain kernel for every instance).
+        item_chains: chains per tensor-core work item (0: automatic; None:
+        keep the current choice)."""
         I = len(self.instances)
         if min_n is None:
             self.ws.tc_enabled = 0
@@ -343,6 +345,8 @@ class PTBatch:
             self.tc_terms = terms
             self._tc_terms_cap = terms
         self.ws.tc_min_n = int(min_n)
+        if item_chains is not None:
+            self.ws.tc_item_chains = int(item_chains)
         check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(ht_), ref(self.ws),
                                         self._stream.cuda_stream), "tc setup")
         self._graphs = {}
@@ -378,42 +382,95 @@ class PTBatch:
         self._setup_tc(self.tc_min_n)
         self.ws.tc_rand_slots = slots
 
-    def autotune(self, sweeps: int = 3, candidates=(64, 256, 512, 1024, None),
-                 seed: int = 1) -> dict:
-        """Choose the tensor-core threshold (instances with n >= threshold
-        take the tensor-core sweep, the rest the plain kernel; None = plain
-        only) by timing `sweeps` sequential sweeps of the current chains per
-        candidate with CUDA events.  The chains are restored afterwards, so
-        results do not depend on the tuning.  Returns {candidate: ms}."""
+    def autotune(self, sweeps: int = 8,
+                 candidates=(64, 256, 512, 1024, None),
+                 item_chains=(0, 0.5, 0.25), unit_sweeps=(0, 4, 16),
+                 exchange_every=(1,), seed: int = 1) -> dict:
+        """Pick the tuning knobs of the sweep by timing them on the current
+        chains (CUDA events; a coordinate search, one knob at a time, each
+        starting from the best of the previous ones):
+
+          candidates      tensor-core threshold: instances with n >= it
+                          take the tensor-core sweep, the rest the plain
+                          kernel (None: plain only)
+          item_chains     chains per tensor-core CTA: 0 automatic, or a
+                          fraction of a CTA's full tensor memory (128 / F)
+          unit_sweeps     sweeps per work unit of the persistent kernel
+                          (0: chosen per launch)
+          exchange_every  replica-exchange interval; only (1,), every
+                          sweep as the reference does, unless the caller
+                          opts in to others
+
+        The chains are restored afterwards, so results do not depend on the
+        tuning.  Returns {candidate threshold: ms per sweep} for the first
+        knob (the threshold); every timing and the choice are kept in
+        self.autotune_report."""
         self.autotune_pending = False
         keep = [self.spins, self.energies, self.beta_idx, self.chain_beta,
                 self.best_energy, self.best_sweep, self.best_spins,
                 self.sweep_counter, self.status, self.ticket, self.fields]
         saved = [t.clone() for t in keep]
         n = np.asarray(self.n)
-        times = {}
-        for c in candidates:
-            if c is not None and not ((n >= max(c, 64)) & (n <= 2048)).any():
-                continue
-            self._setup_tc(c)
-            self.run(1, seed=seed, graph_chunk=0,
-                     final_recompute=False)   # warm-up, attributes
-            st = self._stream
+        st = self._stream
+
+        def timed(k):
+            self.run(k, seed=seed, graph_chunk=0, final_recompute=False,
+                     exchange_every=self._xe)     # warm-up, attributes
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(st)
-            self.run(sweeps, seed=seed, graph_chunk=0, final_recompute=False)
+            self.run(k, seed=seed, graph_chunk=0, final_recompute=False,
+                     exchange_every=self._xe)
             b.record(st)
             b.synchronize()
-            times[c] = a.elapsed_time(b) / sweeps
             for t, v in zip(keep, saved):
                 t.copy_(v)
-        best = min(times, key=times.get)
-        self._setup_tc(best)
+            return a.elapsed_time(b) / k
+
+        report = {"threshold": {}, "item_chains": {}, "unit_sweeps": {},
+                  "exchange_every": {}}
+        self._xe = 1
+        for c in candidates:
+            if c is not None and not ((n >= max(c, 64)) & (n <= 2048)).any():
+                continue
+            self._setup_tc(c, 0)
+            self.ws.tc_unit_sweeps = 0
+            report["threshold"][c] = timed(sweeps)
+        best_c = min(report["threshold"], key=report["threshold"].get)
+        best = {"threshold": best_c, "item_chains": 0, "unit_sweeps": 0,
+                "exchange_every": 1}
+        if best_c is not None:
+            self._setup_tc(best_c, 0)
+            full = int(128 / (1 if n.max() <= 512 else
+                              2 if n.max() <= 1024 else 4))
+            for f in item_chains:
+                ic = 0 if not f else max(int(full * f), 1)
+                if ic in report["item_chains"]:
+                    continue
+                self._setup_tc(best_c, ic)
+                report["item_chains"][ic] = timed(sweeps)
+            best["item_chains"] = min(report["item_chains"],
+                                      key=report["item_chains"].get)
+            self._setup_tc(best_c, best["item_chains"])
+            for u in unit_sweeps:
+                self.ws.tc_unit_sweeps = int(u)
+                report["unit_sweeps"][u] = timed(max(sweeps, 2 * int(u)))
+            best["unit_sweeps"] = min(report["unit_sweeps"],
+                                      key=report["unit_sweeps"].get)
+            self.ws.tc_unit_sweeps = int(best["unit_sweeps"])
+        for xe in exchange_every:
+            self._xe = int(xe)
+            report["exchange_every"][int(xe)] = timed(sweeps)
+        best["exchange_every"] = min(report["exchange_every"],
+                                     key=report["exchange_every"].get)
+        self._xe = best["exchange_every"]
+        if best_c is None:
+            self._setup_tc(None)
         torch.cuda.synchronize(self.device)
         self.autotune_pending = False
-        self.autotune_ms = times
-        return times
+        self.autotune_ms = report["threshold"]
+        self.autotune_report = {"choice": best, "ms_per_sweep": report}
+        return report["threshold"]
 
     def enable_stream_keys(self):
         """Per-chain sweep-stream keys (all 0: the plain streams); accepted
@@ -531,13 +588,15 @@ class PTBatch:
     def run(self, num_sweeps: int, *, seed: int, update: str = "sequential",
             use_pt: bool = True, log_omega: bool = False,
             graph_chunk: int = 128, recompute_every: int | None = None,
-            final_recompute: bool = True):
+            final_recompute: bool = True, exchange_every: int | None = None):
         """Sweeps with exchange.  recompute_every: the tensor-core path
         rebuilds fields and energies from the spins every that many sweeps
         (default 4 when J is not exact in BF16, never otherwise); with
         final_recompute the returned energies are then recomputed once more
         at the end (callers chaining many short runs can skip it and call
-        recompute() once)."""
+        recompute() once).  exchange_every: replica exchange after every
+        sweep (1, the reference's schedule) or only after every k-th (an
+        opt-in knob; None: the autotuner's choice, else 1)."""
         if self.autotune_pending and update == "sequential" and num_sweeps:
             self.autotune()
         if update == "random" and self.tc and num_sweeps:
@@ -553,8 +612,11 @@ class PTBatch:
             self.s.log_omega = _ptr(self.log_omega)
         else:
             self.s.log_omega = 0
+        if exchange_every is None:
+            exchange_every = getattr(self, "_xe", 1)
         opts = _lib.Options(seed & ((1 << 64) - 1), upd, int(use_pt), stride,
-                            int(self.best_global), 0, int(recompute_every))
+                            int(self.best_global), 0, int(recompute_every),
+                            int(exchange_every))
         st = self._stream.cuda_stream
         # first call with zero sweeps sets kernel attributes outside capture
         check(self.lib.pysa_gb_sweeps(ref(self.p), ref(self.s), ref(self.ws),

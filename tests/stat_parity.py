@@ -63,7 +63,24 @@ def compare(arms, label):
         print(f"{label} {k}: KS p={pks:.3f}, hit rates {px:.3f} / {py:.3f} "
               f"(Fisher p={pf:.3f}), slot means min Bonferroni p="
               f"{min(pw, 1.0):.3f}")
+    for name, (best, slots) in arms.items():
+        h = int((best <= target).sum())
+        lo, hi = wilson(h, len(best))
+        se = best.std(ddof=1) / np.sqrt(len(best))
+        print(f"{label} {name}: reads {len(best)}, best energy mean "
+              f"{best.mean():.4f} +- {1.96 * se:.4f} (95 %), hit rate at "
+              f"{target:.4f}: {h / len(best):.3f} [{lo:.3f}, {hi:.3f}], "
+              f"slot 0 (coldest) final energy mean {slots[:, 0].mean():.4f}")
     return report
+
+
+def wilson(k, m, z=1.96):
+    """95 % Wilson score interval of a binomial proportion k / m."""
+    p = k / m
+    d = 1 + z * z / m
+    c = (p + z * z / (2 * m)) / d
+    r = z * np.sqrt(p * (1 - p) / m + z * z / (4 * m * m)) / d
+    return c - r, c + r
 
 
 def assert_same(report, label):

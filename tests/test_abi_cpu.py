@@ -22,14 +22,14 @@ def test_library_exports_every_header_symbol():
     assert len(names) >= 10
     for name in names:
         assert hasattr(lib, name), name
-    assert lib.pysa_gb_abi_version() == 1
+    assert lib.pysa_gb_abi_version() == 2
 
 
 def test_struct_sizes_match_header_layout():
     from pysa_gb300 import _lib
     assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 19 * 8
     assert ctypes.sizeof(_lib.State) == 12 * 8
-    assert ctypes.sizeof(_lib.Options) == 8 + 6 * 4
+    assert ctypes.sizeof(_lib.Options) == 8 + 8 * 4
     assert ctypes.sizeof(_lib.AisOptions) == 8 + 4 * 4 + 8 + 2 * 4
 
 

@@ -26,10 +26,16 @@ The seeds are fixed, so the outcome is deterministic.  The arms gpu/f64
 answer whether the float32 sweeps of a float_type='float64' Solver sample
 the reference's float64 distribution.
 """
+import os
+
 import numpy as np
 import pytest
 
 import stat_parity as sp
+
+# PYSA_GB_STATS_FULL=1: the C1 configuration's own sizes (400 reads, 1000
+# sweeps) instead of the quick test sizes; used for the recorded note
+FULL = os.environ.get("PYSA_GB_STATS_FULL") == "1"
 
 pytestmark = pytest.mark.gpu
 
@@ -68,14 +74,16 @@ def test_sk128_statistically_indistinguishable(oracle):
     """SK N=128, J ~ N(0, 1)/sqrt(N), 32 replicas on T 1.0-3.5 (the C1
     ensemble), 256 reads, 200 sweeps."""
     J = sp.sk(128, 1)
+    Rd, S = (400, 1000) if FULL else (256, 200)
     sp.assert_same(sp.compare(_run_arms(
-        oracle, J, sp.ladder(32, 1.0, 3.5), 256, 200, 100), "sk128"), "sk128")
+        oracle, J, sp.ladder(32, 1.0, 3.5), Rd, S, 100), "sk128"), "sk128")
 
 
 def test_wishart256_statistically_indistinguishable(oracle):
     """Planted Wishart N=256, M=128 (alpha 0.5), 32 replicas on T 0.05-1.0,
     256 reads, 100 sweeps."""
     J = sp.wishart(256, 128, 2)
+    Rd, S = (400, 500) if FULL else (256, 100)
     sp.assert_same(sp.compare(_run_arms(
-        oracle, J, sp.ladder(32, 0.05, 1.0), 256, 100, 200), "wishart256"),
+        oracle, J, sp.ladder(32, 0.05, 1.0), Rd, S, 200), "wishart256"),
         "wishart256")
