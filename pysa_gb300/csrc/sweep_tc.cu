@@ -324,6 +324,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   uint32_t* ex_X = reinterpret_cast<uint32_t*>(dl_s + 5 * CC);
   float* ex_L = dl_s + 9 * CC;
   float* ex_T = dl_s + 13 * CC;
+  // per pair k: the lower slot's replica before the pass, its energy and the
+  // betas' difference ([4][CC] each)
+  int32_t* ex_B2 = reinterpret_cast<int32_t*>(dl_s + 17 * CC);
+  float* ex_E2 = dl_s + 21 * CC;
+  float* ex_D = dl_s + 25 * CC;
   const uint32_t smem_base = smem_addr(smem);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1108,17 +1113,36 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
             }
             __syncwarp();
-            if (lane == 0) {
+            // The pass over pairs (R-1, R-2), (R-2, R-3), ... is serial, but
+            // only the replica entering slot k1 carries from pair to pair:
+            // slot k2 is untouched until pair k.  So every pair's other
+            // replica, its energy and the betas' difference are read by the
+            // lanes up front, and the pass keeps the carried replica and
+            // its energy in registers (same arithmetic, same decisions).
+            int32_t* B2 = ex_B2 + warp * CC;
+            float* E2 = ex_E2 + warp * CC;
+            float* Dk = ex_D + warp * CC;
+            for (int k = lane; k < R - 1; k += 32) {
+              const int k1 = R - k - 1, k2 = R - k - 2;
+              const int b2 = B[k2];
+              B2[k] = b2;
+              E2[k] = E[b2];
+              Dk[k] = __fsub_rn(Bt[k1], Bt[k2]);
+            }
+            __syncwarp();
+            if (lane == 0 && R > 1) {
+              int cb = B[R - 1];
+              float ce = E[cb];
               for (int k = 0; k < R - 1; ++k) {
-                const int k1 = R - k - 1, k2 = R - k - 2;
-                const int b1 = B[k1], b2 = B[k2];
-                const float de = __fmul_rn(__fsub_rn(E[b1], E[b2]),
-                                           __fsub_rn(Bt[k1], Bt[k2]));
-                if (pt_accept_lf(de, Lx[k], X[k])) {
-                  B[k1] = b2;
-                  B[k2] = b1;
-                }
+                const int b2 = B2[k];
+                const float e2 = E2[k];
+                const float de = __fmul_rn(__fsub_rn(ce, e2), Dk[k]);
+                const bool sw = pt_accept_lf(de, Lx[k], X[k]);
+                B[R - k - 1] = sw ? b2 : cb;   // final: no later pair
+                cb = sw ? cb : b2;
+                ce = sw ? ce : e2;
               }
+              B[0] = cb;
             }
             __syncwarp();
             for (int k = lane; k < R; k += 32) {
