@@ -41,8 +41,13 @@ struct TcCfg {
   static constexpr int CC = 128 / F;          // chains per CTA
   static constexpr int NS = (F == 1 || RND) ? 2 : 3;   // B ring stages
   static constexpr int WORDS = 16 * F;        // spin words per chain
+  // A operand: ONE copy of the CC chains' delta rows (physical rows
+  // 128 - CC ... 127) with 128 - CC zero rows on either side; slice q's
+  // 128-row MMA operand starts (128 - CC - q CC) rows in, so only its own
+  // chains' rows fall on its lanes.  K = 64 BF16 = 128 bytes per row.
+  static constexpr int A_ROWS = F == 1 ? 128 : 256 - CC;
   static constexpr size_t A_OFF = 0;
-  static constexpr size_t A_BYTES = (size_t)F * 16384;
+  static constexpr size_t A_BYTES = (size_t)A_ROWS * 128;
   static constexpr size_t B_OFF = A_OFF + A_BYTES;
   static constexpr size_t B_STAGE = 32768;
   static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
@@ -531,10 +536,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 const uint32_t b16 = bf16_bits(v);
                 if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
               }
-#pragma unroll
-              for (int qq = 0; qq < F; ++qq) {
-                const int m = qq * CC + c;
-                unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
+              {
+                const int m = 128 - CC + c;  // chain c's physical A row
+                unsigned char* rowp = smem + C::A_OFF +
                                       ((m >> 3) * 8) * 128 + (m & 7) * 16;
 #pragma unroll
                 for (int kc = 0; kc < 8; ++kc)
@@ -681,22 +685,20 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           go = __all_sync(0xffffffffu, go);
           const bool lead = go && c == 0;
           if (lead) stamp(a, Gb, 0);
-          // one sub-block's deltas of chain c into its A rows of every slice
+          // one sub-block's deltas of chain c into its A row (one copy,
+          // seen by every slice's MMA)
           auto put_a = [&](int gg, const float* d) {
             uint32_t pkg[8];
 #pragma unroll
             for (int j = 0; j < 16; j += 2)
               pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
-#pragma unroll
-            for (int qq = 0; qq < F; ++qq) {
-              const int m = qq * CC + c;
-              unsigned char* rowp = smem + C::A_OFF + qq * 16384 +
-                                    ((m >> 3) * 8) * 128 + (m & 7) * 16;
-              *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
-                  make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
-              *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
-                  make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
-            }
+            const int m = 128 - CC + c;
+            unsigned char* rowp = smem + C::A_OFF + ((m >> 3) * 8) * 128 +
+                                  (m & 7) * 16;
+            *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
+                make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+            *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
+                make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
           };
           if (go) {
             tc::fence_after_sync();
@@ -1208,7 +1210,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           const uint32_t idesc = r_hi - r_lo == 256
                                      ? idesc_full
                                      : tc::idesc_bf16(128, r_hi - r_lo);
-          const uint32_t a0 = smem_base + (uint32_t)(C::A_OFF + qq * 16384);
+          // slice qq's view: 128 rows starting (128 - CC - qq CC) rows in
+          const uint32_t a0 =
+              smem_base + (uint32_t)(C::A_OFF +
+                                     (size_t)((128 - CC - qq * CC) >> 3) * 1024);
           const uint32_t b0 = smem_base +
                               (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
                               (uint32_t)(r_lo / 8) * 1024u;
