@@ -107,6 +107,15 @@ typedef struct {
   const int32_t *csr_rows;    /* 9 int32 per row */
   const int32_t *csr_col;     /* column of each entry */
   const float *csr_val;       /* coupling of each entry */
+  int32_t csr_width;          /* layout of the sparse rows, as
+                                 pysa_gb_workspace.csr_width (0 grouped rows,
+                                 4/8/16/32 fixed records); read by
+                                 pysa_gb_prepare and pysa_gb_energy64_tables,
+                                 which take sparse instances' fields and
+                                 energies from these rows (their dense J is
+                                 never read: j_off may point anywhere, ld >=
+                                 n) */
+  int32_t pad_;
 } pysa_gb_problems;
 
 /* Chain state, updated in place by the sweeps. */

@@ -28,7 +28,7 @@ class Problems(ctypes.Structure):
                 ("ladder_off", P), ("read_inst", P), ("J", P), ("h", P),
                 ("ladder", P), ("ladder_sorted", P), ("csr_row_off", P),
                 ("csr_ent_off", P), ("csr_rows", P), ("csr_col", P),
-                ("csr_val", P)]
+                ("csr_val", P), ("csr_width", I32), ("pad_", I32)]
 
 
 class State(ctypes.Structure):

@@ -255,6 +255,22 @@ int pysa_gb_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
     const int sms = sm_count();
     while (cpb > 32 && (sparse_chains + cpb - 1) / cpb < sms) cpb /= 2;
   }
+  // the sparse-row sweep keeps every chain's spin words (and, in random
+  // order, the visiting order and a record slab) in shared memory
+  {
+    const size_t words = (size_t)(p->max_n + 31) / 32;
+    auto smem = [&](int ch) {
+      return words * ch * 4 + (size_t)p->max_n * 4 + 17408 + 1024;
+    };
+    bool any_sparse = false;
+    for (int i = 0; i < p->num_instances; ++i)
+      any_sparse |= is_sparse(host, i);
+    while (cpb > 32 && smem(cpb) > 232448) cpb /= 2;
+    if (any_sparse && smem(cpb) > 232448)
+      return fail(PYSA_GB_ERR_SIZE,
+                  "sparse instances: n too large for the sparse-row sweep's "
+                  "shared memory at 32 chains per CTA");
+  }
   ws->csr_chains = cpb;
   for (int i = 0; i < p->num_instances; ++i) {
     if (!is_sparse(host, i)) continue;
@@ -818,6 +834,10 @@ int pysa_gb_load_problem(const pysa_gb_problems* p,
   const int n = host->n[inst], ld = host->ld[inst];
   if (n < 1 || p_ld < n || ld < n)
     return fail(PYSA_GB_ERR_ARG, "load_problem: bad sizes");
+  if (is_sparse(host, inst))
+    return fail(PYSA_GB_ERR_ARG,
+                "load_problem: dense problems only (a sparse instance keeps "
+                "no dense couplings)");
   launch_load_problem(*p, inst, n, ld, P, p_ld, (cudaStream_t)stream);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "load_problem");

@@ -36,6 +36,40 @@ void launch_pack_rows(const float* J, int ld, int n, int nc, int ls,
 // (pysa/ising.py:37, pysa/qubo.py:37), summed per lane, then over the warp,
 // then over the chunks in order, so the result does not depend on timing.
 constexpr int kFieldWarps = 8;
+
+// Sparse instances: f_i = sum over row i's stored entries of J_ij s_j in f64
+// (the products are exact; padding entries have value 0), from the fixed
+// records (width > 0: entries csr_ent_off + width i ...) or the grouped
+// rows (csr_rows, 9 offsets per row).
+__device__ __forceinline__ double csr_row_dot(const pysa_gb_problems& p,
+                                              int inst, int i,
+                                              const uint32_t* sw,
+                                              bool ising) {
+  const int64_t eo = p.csr_ent_off[inst];
+  int64_t beg, end;
+  if (p.csr_width > 0) {
+    beg = eo + (int64_t)p.csr_width * i;
+    end = beg + p.csr_width;
+  } else {
+    const int32_t* r = p.csr_rows + 9 * (p.csr_row_off[inst] + i);
+    beg = eo + r[0];
+    end = eo + r[8];
+  }
+  double f = 0.0;
+  for (int64_t e = beg; e < end; ++e) {
+    const int j = p.csr_col[e] & 0x7fffffff;
+    const float sj = ((sw[j >> 5] >> (j & 31)) & 1u) ? 1.0f
+                                                     : (ising ? -1.0f : 0.0f);
+    f += (double)(p.csr_val[e] * sj);
+  }
+  return f;
+}
+
+__device__ __forceinline__ bool is_sparse_inst(const pysa_gb_problems& p,
+                                               int inst) {
+  return p.csr_row_off && p.csr_row_off[inst] >= 0;
+}
+
 __global__ void __launch_bounds__(32 * kFieldWarps) k_fields(const PrepArgs a) {
   __shared__ double e_s[kFieldWarps];
   const int64_t c = blockIdx.x;
@@ -54,6 +88,24 @@ __global__ void __launch_bounds__(32 * kFieldWarps) k_fields(const PrepArgs a) {
   const float* h = a.p.h + a.p.h_off[inst];
   const uint32_t* sw = a.s.spins + c * a.p.words;
   double e = 0.0;
+  if (is_sparse_inst(a.p, inst)) {  // uniform per CTA
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double f = csr_row_dot(a.p, inst, i, sw, ising);
+      const uint32_t bit = (sw[i >> 5] >> (i & 31)) & 1u;
+      const double si = bit ? 1.0 : (ising ? -1.0 : 0.0);
+      e += si * (0.5 * f + (double)h[i]);
+      a.fields[c * a.field_ld + i] = (float)(f + (double)h[i]);
+    }
+    e = warp_sum(e);
+    if (lane == 0) e_s[warp] = e;
+    __syncthreads();
+    if (threadIdx.x == 0 && a.set_energies) {
+      double t = 0.0;
+      for (int w = 0; w < nwarps; ++w) t += e_s[w];
+      a.s.energies[c] = (float)t;
+    }
+    return;
+  }
   constexpr int TC = 8;  // columns per lane per chunk
   for (int base = 256 * warp; base < n; base += 256 * nwarps) {
     double F[TC];
@@ -339,12 +391,39 @@ __global__ void __launch_bounds__(256) k_energy64(
 }
 
 // Same with instance inst's f32 couplings and fields of the problem tables.
+// Sparse instances from their stored rows (thread per row, fixed
+// reduction order).
 __global__ void __launch_bounds__(256) k_energy64_tables(
     const pysa_gb_problems p, int inst, const uint32_t* spins, int words,
     double* out) {
-  energy64_body<float>(p.problem_type, p.n[inst], p.ld[inst],
-                       p.J + p.j_off[inst], p.h + p.h_off[inst], spins, words,
-                       out);
+  if (!is_sparse_inst(p, inst)) {
+    energy64_body<float>(p.problem_type, p.n[inst], p.ld[inst],
+                         p.J + p.j_off[inst], p.h + p.h_off[inst], spins,
+                         words, out);
+    return;
+  }
+  __shared__ double e_s[8];
+  const int64_t c = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t* sw = spins + c * words;
+  const bool ising = p.problem_type == PYSA_GB_ISING;
+  const int n = p.n[inst];
+  const float* h = p.h + p.h_off[inst];
+  double e = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double si =
+        ((sw[i >> 5] >> (i & 31)) & 1u) ? 1.0 : (ising ? -1.0 : 0.0);
+    if (si != 0.0) e += si * (0.5 * csr_row_dot(p, inst, i, sw, ising) +
+                              (double)h[i]);
+  }
+  e = warp_sum(e);
+  if (lane == 0) e_s[warp] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += e_s[w];
+    out[c] = t;
+  }
 }
 
 void launch_energy64(int ptype, int n, int ld, const double* J,

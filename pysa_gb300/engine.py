@@ -41,6 +41,10 @@ def unpack_spins(words_arr: np.ndarray, n: int, problem_type: str,
     return bits.astype(dtype)
 
 
+def _dense(J) -> np.ndarray:
+    return J.toarray() if hasattr(J, "toarray") else np.asarray(J)
+
+
 def bf16_exact(a: np.ndarray) -> bool:
     """True when every value is exactly representable in bfloat16."""
     u = np.ascontiguousarray(a, np.float32).view(np.uint32)
@@ -53,18 +57,29 @@ def csr_tables(J: np.ndarray):
     its nonzero entries grouped by column % 8, ascending column inside a
     group.  Returns rows [n, 9] int32 (group starts and the row end), col
     int32 and val float32."""
-    Jt = np.ascontiguousarray(np.asarray(J, np.float32).T)
-    n = Jt.shape[0]
-    r, c = np.nonzero(Jt)
-    g = c & 7
-    order = np.lexsort((c, g, r))
-    r, c, g = r[order], c[order], g[order]
+    if hasattr(J, "tocoo"):  # scipy.sparse: never densified
+        T = J.T.tocoo()
+        n = T.shape[0]
+        keep = T.data != 0
+        r = T.row[keep].astype(np.int64)
+        c = T.col[keep].astype(np.int64)
+        v = T.data[keep].astype(np.float32)
+        g = c & 7
+        order = np.lexsort((c, g, r))
+        r, c, g, v = r[order], c[order], g[order], v[order]
+    else:
+        Jt = np.ascontiguousarray(np.asarray(J, np.float32).T)
+        n = Jt.shape[0]
+        r, c = np.nonzero(Jt)
+        g = c & 7
+        order = np.lexsort((c, g, r))
+        r, c, g = r[order], c[order], g[order]
+        v = Jt[r, c].astype(np.float32)
     cnt = np.zeros(8 * n, np.int64)
     np.add.at(cnt, 8 * r + g, 1)
     starts = np.concatenate([[0], np.cumsum(cnt)])
     rows = starts[8 * np.arange(n)[:, None] + np.arange(9)[None, :]]
-    return (rows.astype(np.int32), c.astype(np.int32),
-            Jt[r, c].astype(np.float32))
+    return rows.astype(np.int32), c.astype(np.int32), v
 
 
 def csr_records(J: np.ndarray, width: int):
@@ -90,10 +105,21 @@ def csr_records(J: np.ndarray, width: int):
     return (c & 0xFFFFFFFF).astype(np.uint32).view(np.int32), v
 
 
-def mean_degree(J: np.ndarray) -> float:
-    """Nonzero couplings per row."""
+def mean_degree(J) -> float:
+    """Nonzero couplings per row (dense array or scipy.sparse matrix)."""
+    if hasattr(J, "tocoo"):
+        return float(J.count_nonzero()) / max(J.shape[0], 1)
     J = np.asarray(J)
     return float(np.count_nonzero(J)) / max(J.shape[0], 1)
+
+
+def max_degree(J) -> int:
+    """Most nonzero couplings in a column (dense or scipy.sparse)."""
+    if hasattr(J, "tocoo"):
+        T = J.tocsc()
+        T.eliminate_zeros()
+        return int(np.diff(T.indptr).max(initial=0))
+    return int(np.count_nonzero(J, axis=0).max(initial=0))
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -102,7 +128,9 @@ def _ptr(t: torch.Tensor) -> int:
 
 @dataclass
 class Instance:
-    J: np.ndarray       # [n, n] couplings, zero diagonal
+    J: np.ndarray       # [n, n] couplings, zero diagonal; a scipy.sparse
+    #                     matrix is taken as is for sparse-row instances
+    #                     (never densified), densified otherwise
     h: np.ndarray       # [n]
     ladder: np.ndarray  # [R] betas in slot order
     reads: int
@@ -138,6 +166,18 @@ class PTBatch:
         self.ptype = _lib.ISING if problem_type == "ising" else _lib.QUBO
         I = len(instances)
         self.instances = instances
+        # sparse-row instances and their tables
+        if sparse is None or sparse is False:
+            flags = [False] * I
+        elif sparse is True:
+            flags = [True] * I
+        elif sparse == "auto":
+            flags = [mean_degree(x.J) <= max(8.0, len(x.h) / 64)
+                     for x in instances]
+        else:
+            flags = [bool(f) for f in sparse]
+            if len(flags) != I:
+                raise ValueError("sparse: one flag per instance")
         n = np.array([len(x.h) for x in instances], np.int32)
         R = np.array([len(x.ladder) for x in instances], np.int32)
         Rd = np.array([x.reads for x in instances], np.int32)
@@ -152,7 +192,8 @@ class PTBatch:
         for i in range(I):
             j_off[i], h_off[i], ladder_off[i] = jt, ht, lt
             chain_off[i], read_off[i] = ct, rt
-            jt += int(n[i]) * int(ld[i])
+            if not flags[i]:  # sparse instances keep no dense couplings
+                jt += int(n[i]) * int(ld[i])
             ht += int(n[i])
             lt += int(R[i])
             ct += int(R[i]) * int(Rd[i])
@@ -168,28 +209,18 @@ class PTBatch:
         lsort = np.zeros(max(lt, 1), np.int32)
         for i, x in enumerate(instances):
             ni, li = int(n[i]), int(ld[i])
-            blk = np.zeros((ni, li), np.float32)
-            # transposed: row j = change of every field when spin j flips
-            blk[:, :ni] = np.asarray(x.J, np.float32).T
-            Jcat[j_off[i]:j_off[i] + ni * li] = blk.ravel()
+            if not flags[i]:
+                blk = np.zeros((ni, li), np.float32)
+                # transposed: row j = change of every field when spin j flips
+                blk[:, :ni] = np.asarray(_dense(x.J), np.float32).T
+                Jcat[j_off[i]:j_off[i] + ni * li] = blk.ravel()
             hcat[h_off[i]:h_off[i] + ni] = np.asarray(x.h, np.float32)
             lad[ladder_off[i]:ladder_off[i] + R[i]] = x.ladder
             lsort[ladder_off[i]:ladder_off[i] + R[i]] = np.argsort(
                 np.asarray(x.ladder, np.float32), kind="stable")
         read_inst = np.repeat(np.arange(I, dtype=np.int32), Rd)
         dev = self.device
-        # sparse-row instances and their tables
-        if sparse is None or sparse is False:
-            flags = [False] * I
-        elif sparse is True:
-            flags = [True] * I
-        elif sparse == "auto":
-            flags = [mean_degree(x.J) <= max(8.0, len(x.h) / 64)
-                     for x in instances]
-        else:
-            flags = [bool(f) for f in sparse]
-            if len(flags) != I:
-                raise ValueError("sparse: one flag per instance")
+        # sparse-row instances and their tables (flags above)
         self.sparse = np.asarray(flags, np.int32) if I else np.zeros(
             1, np.int32)
         row_off = np.full(max(I, 1), -1, np.int64)
@@ -197,7 +228,7 @@ class PTBatch:
         rows_l, col_l, val_l = [], [], []
         nr, ne = 0, 0
         # fixed records when every sparse row has at most 32 entries
-        maxdeg = max([int(np.count_nonzero(x.J, axis=0).max(initial=0))
+        maxdeg = max([max_degree(x.J)
                       for i, x in enumerate(instances) if flags[i]] or [0])
         self.csr_width = next((w for w in (4, 8, 16, 32) if maxdeg <= w), 0)
         for i, x in enumerate(instances):
@@ -247,6 +278,7 @@ class PTBatch:
             for k in ("csr_row_off", "csr_ent_off", "csr_rows", "csr_col",
                       "csr_val"):
                 setattr(self.p, k, _ptr(t[k]))
+            self.p.csr_width = self.csr_width
         C, W = max(ct, 1), self.words
         z = lambda *s, dt: torch.zeros(*s, dtype=dt, device=dev)  # noqa: E731
         self.spins = z(C, W, dt=torch.int32)
@@ -319,7 +351,7 @@ class PTBatch:
         ht_ = self._ht
         if not hasattr(self, "tc_b"):
             # sized once for the widest selection (every instance >= 64)
-            terms = 1 if all(bf16_exact(x.J) for i, x in
+            terms = 1 if all(bf16_exact(_dense(x.J)) for i, x in
                              enumerate(self.instances)
                              if not self.sparse[i]) else 2
             if self._tc_terms_req is not None:

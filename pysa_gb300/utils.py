@@ -58,10 +58,18 @@ def problem_from_triplets(rows, cols, vals, n: int | None = None):
     return (M + M.T) / 2.0
 
 
-def lattice_adjacency(m: int, n: int) -> np.ndarray:
+def lattice_adjacency(m: int, n: int, sparse: bool = False):
     """Adjacency of the m x n lattice with open boundaries, site (i, j) at
-    index i * n + j."""
+    index i * n + j: a dense array, or with sparse=True a scipy.sparse CSR
+    matrix (for lattices whose dense form would not fit in host memory)."""
     idx = np.arange(m * n).reshape(m, n)
+    if sparse:
+        import scipy.sparse as sps
+        r = np.concatenate([idx[1:, :].ravel(), idx[:-1, :].ravel(),
+                            idx[:, 1:].ravel(), idx[:, :-1].ravel()])
+        c = np.concatenate([idx[:-1, :].ravel(), idx[1:, :].ravel(),
+                            idx[:, :-1].ravel(), idx[:, 1:].ravel()])
+        return sps.csr_matrix((np.ones(len(r)), (r, c)), shape=(m * n, m * n))
     A = np.zeros((m * n, m * n))
     A[idx[1:, :].ravel(), idx[:-1, :].ravel()] = 1
     A[idx[:-1, :].ravel(), idx[1:, :].ravel()] = 1

@@ -27,7 +27,7 @@ def test_library_exports_every_header_symbol():
 
 def test_struct_sizes_match_header_layout():
     from pysa_gb300 import _lib
-    assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 19 * 8
+    assert ctypes.sizeof(_lib.Problems) == 4 * 4 + 2 * 8 + 19 * 8 + 2 * 4
     assert ctypes.sizeof(_lib.State) == 12 * 8
     assert ctypes.sizeof(_lib.Options) == 8 + 8 * 4
     assert ctypes.sizeof(_lib.AisOptions) == 8 + 4 * 4 + 8 + 2 * 4

@@ -151,3 +151,87 @@ def test_sparse_log_omega_and_solver_auto():
         assert (ra["states"] == rb["states"]).all()
         assert ra["best_energy"] == rb["best_energy"]
         assert ra["log_Zf"] == rb["log_Zf"]
+
+
+def test_sparse_storage_prepare_and_energies_from_rows(oracle):
+    """Sparse instances keep no dense couplings on the device: their fields
+    and energies (pysa_gb_prepare) and their f64 energies
+    (pysa_gb_energy64_tables) come from the stored rows, equal to the
+    oracle's f64 energies for integer couplings.  n = 9216 (a 96 x 96
+    lattice with integer couplings) also takes the sparse sweep past the
+    register-resident kernel's 4096 spins, in both orders."""
+    import torch
+    from pysa_gb300 import Instance, PTBatch, pack_spins, unpack_spins, _lib
+    from pysa_gb300._lib import check, ref
+    from pysa_gb300.utils import lattice_adjacency
+    rng = np.random.default_rng(12)
+    L = 96
+    A = lattice_adjacency(L, L, sparse=True).tocoo()
+    w = rng.integers(-3, 4, A.nnz)
+    upper = A.row < A.col
+    import scipy.sparse as sps
+    U = sps.coo_matrix((w[upper], (A.row[upper], A.col[upper])),
+                       shape=A.shape)
+    Jsp = (U + U.T).tocsr().astype(np.float32)
+    n = L * L
+    h = rng.integers(-2, 3, n).astype(np.float32)
+    R, Rd = 4, 2
+    betas = (1.0 / np.geomspace(0.5, 3.0, R)).astype(np.float32)
+    x0 = _states(rng, "ising", (Rd, R, n))
+    Jd = Jsp.toarray()
+    e0 = np.array([[oracle.energy64(Jd, h, s) for s in r] for r in x0])
+    for update in ("sequential", "random"):
+        b = PTBatch("ising", [Instance(Jsp, h, betas, Rd)], sparse=True,
+                    perm_slots=2)
+        assert b._t["J"].numel() == 1      # no dense couplings stored
+        b.set_states(pack_spins(x0, "ising", b.words), None)
+        got_e0 = b.energies.cpu().numpy().reshape(Rd, R)
+        assert np.array_equal(got_e0, e0.astype(np.float32))
+        b.run(2, seed=21, update=update)
+        r = b.fetch()
+        want = oracle.pt_run("ising", Jd, h, betas, x0,
+                             e0.astype(np.float32),
+                             np.tile(np.arange(R, dtype=np.int32), (Rd, 1)),
+                             seed=21, num_sweeps=2, update=update)
+        sp = unpack_spins(r["spins"].reshape(Rd, R, -1), n, "ising",
+                          np.float32)
+        assert (sp == want["spins"]).all(), update
+        assert (r["energies"].reshape(Rd, R) == want["energies"]).all()
+        # f64 energies of the returned states from the stored rows
+        out = torch.empty(Rd * R, dtype=torch.float64, device=b.device)
+        check(_lib.load().pysa_gb_energy64_tables(
+            ref(b.p), ref(b._ht), 0, b.spins.data_ptr(), b.words, Rd * R,
+            out.data_ptr(), b._stream.cuda_stream), "energy64_tables")
+        e64 = np.array([oracle.energy64(Jd, h, s)
+                        for s in want["spins"].reshape(-1, n)])
+        assert np.array_equal(out.cpu().numpy(), e64)
+
+
+def test_lattice128_sparse_storage():
+    """The 128 x 128 lattice (16 384 spins) of the Ising tutorial's kind
+    runs from a scipy.sparse problem without any dense copy: returned
+    energies equal the exact energies of the returned states, and each
+    chain's best energy is its best state's energy."""
+    from pysa_gb300 import Instance, PTBatch, pack_spins, unpack_spins
+    from pysa_gb300.utils import lattice_adjacency
+    L = 128
+    J = (-lattice_adjacency(L, L, sparse=True)).astype(np.float32)
+    n = L * L
+    h = np.zeros(n, np.float32)
+    R, Rd = 8, 4
+    betas = (1.0 / np.geomspace(1.0, 3.5, R)).astype(np.float32)
+    rng = np.random.default_rng(13)
+    x0 = _states(rng, "ising", (Rd, R, n))
+    for update in ("sequential", "random"):
+        b = PTBatch("ising", [Instance(J, h, betas, Rd)], sparse=True,
+                    perm_slots=2)
+        assert b._t["J"].numel() == 1
+        b.set_states(pack_spins(x0, "ising", b.words), None)
+        b.run(5, seed=3, update=update)
+        r = b.fetch()
+        S = unpack_spins(r["spins"], n, "ising", np.float64)
+        E = np.einsum("ri,ri->r", S, (J @ S.T).T) / 2 + S @ h
+        assert np.array_equal(r["energies"].astype(np.float64), E)
+        B = unpack_spins(r["best_spins"], n, "ising", np.float64)
+        Eb = np.einsum("ri,ri->r", B, (J @ B.T).T) / 2 + B @ h
+        assert np.array_equal(r["best_energy"].astype(np.float64), Eb)
