@@ -45,7 +45,13 @@ struct TcCfg {
   // 128 - CC ... 127) with 128 - CC zero rows on either side; slice q's
   // 128-row MMA operand starts (128 - CC - q CC) rows in, so only its own
   // chains' rows fall on its lanes.  K = 64 BF16 = 128 bytes per row.
-  static constexpr int A_ROWS = F == 1 ? 128 : 256 - CC;
+  // fold 4: two A buffers (block t writes buffer t & 1 while the MMAs of
+  // block t - 1 still read the other), interleaved with the zero rows:
+  // [zero][buffer 0][zero][buffer 1][zero]; buffer b's delta rows are
+  // 128 - CC + 128 b ...
+  static constexpr int A_NBUF = F == 4 ? 2 : 1;
+  static constexpr int A_ROWS =
+      F == 1 ? 128 : (A_NBUF == 2 ? 384 - CC : 256 - CC);
   static constexpr size_t A_OFF = 0;
   static constexpr size_t A_BYTES = (size_t)A_ROWS * 128;
   static constexpr size_t B_OFF = A_OFF + A_BYTES;
@@ -79,8 +85,8 @@ struct TcCfg {
   static constexpr size_t POSB_BYTES = RND ? (size_t)2 * 2 * CC * 4 : 0;
   static constexpr size_t BAR_OFF = (POSB_OFF + POSB_BYTES + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
-  // lf_full[2], lf_free[2], full[NS], free[NS], drain
-  static constexpr int NBARS = 14 + 2 * NS;
+  // lf_full[2], lf_free[2], full[NS], free[NS], drain, mma_done_b[2]
+  static constexpr int NBARS = 16 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
   // tmem slot, abort flag, current unit
   static constexpr size_t BYTES = MISC_OFF + 24;
@@ -89,7 +95,7 @@ struct TcCfg {
 
 struct TcShared {
   uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *rc_full,
-      *rc_done, *lf_full, *lf_free, *full, *free_, *drain;
+      *rc_done, *lf_full, *lf_free, *full, *free_, *drain, *mma_done_b;
   uint32_t* tmem_slot;
   volatile int32_t* abort;
 };
@@ -119,6 +125,23 @@ __device__ __forceinline__ void drain_wait(uint64_t* bar, uint32_t parity) {
   const uint64_t t0 = globaltimer_ns();
   while (!mbar_try_wait(bar, parity))
     if (globaltimer_ns() - t0 > 1000000000ull) return;
+}
+
+// Every MMA up to and including block Gx has completed.  One A buffer: the
+// per-block barrier, at most one phase behind (each block waits for its
+// predecessor's MMAs before writing A).  Two A buffers (fold 4): blocks Gx
+// and Gx - 1 may both be pending, and a parity wait on the per-block
+// barrier cannot tell their phases apart, so the per-buffer barriers are
+// waited instead (their latest phases are these blocks').
+template <int NBUF>
+__device__ __forceinline__ bool mmas_done_through(uint32_t Gx,
+                                                  const TcShared& sh,
+                                                  int32_t* status) {
+  if (NBUF == 1) return tc_wait(sh.mma_done, Gx & 1, sh, status);
+  if (!tc_wait(&sh.mma_done_b[Gx & 1], (Gx >> 1) & 1, sh, status))
+    return false;
+  return Gx == 0 || tc_wait(&sh.mma_done_b[(Gx - 1) & 1],
+                            ((Gx - 1) >> 1) & 1, sh, status);
 }
 
 // (sum, compensation) + x with Neumaier's compensated summation in f32
@@ -306,6 +329,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   sh.full = bars + 13;
   sh.free_ = bars + 13 + C::NS;
   sh.drain = bars + 13 + 2 * C::NS;
+  sh.mma_done_b = bars + 14 + 2 * C::NS;  // [2]: MMAs of blocks using A
+                                          // buffer 0 / 1 (two buffers)
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
   volatile int32_t* unit_s =
@@ -516,7 +541,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           // ========================================== recompute: A = spins
           // the previous sweep's MMAs (which read A) must be done
           bool rok = true;
-          if (s > 0) rok = tc_wait(sh.mma_done, (Gs - 1) & 1, sh, status);
+          if (s > 0) rok = mmas_done_through<C::A_NBUF>(Gs - 1, sh, status);
           for (int t = 0; t < NB; ++t) {
             const uint32_t R_ = RG + (uint32_t)t;
             bool go = rok && q == 0 && !*sh.abort;
@@ -685,6 +710,14 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           go = __all_sync(0xffffffffu, go);
           const bool lead = go && c == 0;
           if (lead) stamp(a, Gb, 0);
+          // fold 4: block Gb's A buffer is free once the MMAs of block
+          // Gb - 2 (its previous user) are done; a unit's first two blocks
+          // follow the previous unit's, whose MMAs have all completed
+          auto a_buffer_free = [&]() {
+            return Gb < G0 + 2 ||
+                   tc_wait(&sh.mma_done_b[Gb & 1], ((Gb >> 1) - 1) & 1, sh,
+                           status);
+          };
           // one sub-block's deltas of chain c into its A row (one copy,
           // seen by every slice's MMA)
           auto put_a = [&](int gg, const float* d) {
@@ -692,7 +725,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
             for (int j = 0; j < 16; j += 2)
               pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
-            const int m = 128 - CC + c;
+            const int m = 128 - CC + c + (C::A_NBUF == 2 ? 128 * (int)(Gb & 1) : 0);
             unsigned char* rowp = smem + C::A_OFF + ((m >> 3) * 8) * 128 +
                                   (m & 7) * 16;
             *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
@@ -912,9 +945,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 // sub-blocks 0-2 go to the other slices' warps; the last
                 // sub-block's rows here, after the previous block's MMAs
                 if (g == 2) named_arrive_aput();
-                if (g == 3 && (Gb == G0 || tc_wait(sh.mma_done, (Gb - 1) & 1,
-                                                   sh, status)))
-                  put_a(3, dcur);
+                if (g == 3 && a_buffer_free()) put_a(3, dcur);
               } else {
                 if (g == 1)
                   a_early =
@@ -977,7 +1008,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             named_sync_aput();
             const int hr = (q + 3 - qt) & 3;  // 0, 1, 2 for q = qt+1, +2, +3
             if (hr < 3 && __all_sync(0xffffffffu, !*sh.abort) &&
-                (Gb == G0 || tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status))) {
+                a_buffer_free()) {
               float d[16];
 #pragma unroll
               for (int j = 0; j < 16; ++j) d[j] = dl_s[(16 * hr + j) * CC + c];
@@ -1159,7 +1190,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
       }  // sweeps
 
       // ----------------------------------------------------------- epilogue
-      if (!*sh.abort) tc_wait(sh.mma_done, (Gend - 1) & 1, sh, status);
+      if (!*sh.abort) mmas_done_through<C::A_NBUF>(Gend - 1, sh, status);
       tc::fence_after_sync();
       if (threadIdx.x == 0) stamp_cta(a, 2);
       if (__all_sync(0xffffffffu, !*sh.abort)) {
@@ -1205,15 +1236,16 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
         // rows [r_lo, r_hi) of the 256-row B tile in `slot` against A slice
         // qq, into the field columns 256 j + r_lo ...
         auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi,
-                            uint32_t acc) {
+                            uint32_t acc, int ab) {
           if (r_hi <= r_lo) return;
           const uint32_t idesc = r_hi - r_lo == 256
                                      ? idesc_full
                                      : tc::idesc_bf16(128, r_hi - r_lo);
           // slice qq's view: 128 rows starting (128 - CC - qq CC) rows in
           const uint32_t a0 =
-              smem_base + (uint32_t)(C::A_OFF +
-                                     (size_t)((128 - CC - qq * CC) >> 3) * 1024);
+              smem_base +
+              (uint32_t)(C::A_OFF +
+                         (size_t)((128 - CC - qq * CC + 128 * ab) >> 3) * 1024);
           const uint32_t b0 = smem_base +
                               (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
                               (uint32_t)(r_lo / 8) * 1024u;
@@ -1246,7 +1278,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                     }
                     tc::fence_after_sync();
                     mma_rows(slot, qq, j, 0, width,
-                             (t | term | qq) ? 1u : 0u);
+                             (t | term | qq) ? 1u : 0u, 0);
                     tc::commit(&sh.free_[slot]);
                     ++u;
                   }
@@ -1273,6 +1305,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             }
             stamp(a, Gb, 5);
             tc::fence_after_sync();
+            const int ab = C::A_NBUF == 2 ? (int)(Gb & 1) : 0;
             for (int jj = 0; jj < NT && ok; ++jj) {
               const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
               const int width = S - 256 * j < 256 ? S - 256 * j : 256;
@@ -1292,9 +1325,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   }
                   tc::fence_after_sync();
                   if (crit)
-                    mma_rows(slot, qq, j, r0, r0 + 64, 1u);
+                    mma_rows(slot, qq, j, r0, r0 + 64, 1u, ab);
                   else
-                    mma_rows(slot, qq, j, 0, width, 1u);
+                    mma_rows(slot, qq, j, 0, width, 1u, ab);
                 }
                 if (!ok) break;
                 if (crit) {
@@ -1303,8 +1336,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   stamp(a, Gb, 6);
                   for (int term = 0; term < T; ++term) {
                     const uint32_t slot = (u + term) % C::NS;
-                    mma_rows(slot, qq, j, 0, r0, 1u);
-                    mma_rows(slot, qq, j, r0 + 64, width, 1u);
+                    mma_rows(slot, qq, j, 0, r0, 1u, ab);
+                    mma_rows(slot, qq, j, r0 + 64, width, 1u, ab);
                   }
                 }
                 for (int term = 0; term < T; ++term)
@@ -1318,6 +1351,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               if (RND) stamp(a, Gb, 6);
             }
             tc::commit(sh.mma_done);
+            if (C::A_NBUF == 2) tc::commit(&sh.mma_done_b[Gb & 1]);
           }
         }
         if (!ok) *sh.abort = 1;
