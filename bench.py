@@ -254,10 +254,18 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def _timed_oracle():
+    """The oracle's tuned build (oracle/Makefile: same source and arithmetic
+    as the parity build, compiled for the host CPU) for the timed CPU legs."""
+    from oracle import oracle
+    oracle.use_build("timed")
+    oracle.build()
+    return oracle
+
+
 def cpu_reference(w, ptype, P, reads, sweeps, nthreads=0):
     """Oracle (CPU restatement, OpenMP over chains) on `reads` reads."""
-    from oracle import oracle
-    oracle.build()
+    oracle = _timed_oracle()
     h = np.diag(P).astype(np.float32).copy()
     J = P.copy()
     np.fill_diagonal(J, 0)
@@ -556,8 +564,7 @@ def run_batch_workload(args, w, rank, world):
                            "download"}
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
-        from oracle import oracle
-        oracle.build()
+        oracle = _timed_oracle()
         k = int(np.argsort(sizes)[len(sizes) // 2])   # median-size instance
         n = int(sizes[k])
         xs = (2 * srng.integers(0, 2, (8, R, n)) - 1).astype(np.float32)
@@ -889,8 +896,7 @@ def run_reference_ais(args, w, rank, world):
     instance of the workload, all host threads over samples."""
     if rank != 0:
         return 0
-    from oracle import oracle
-    oracle.build()
+    oracle = _timed_oracle()
     n = w["n"]
     rng = np.random.default_rng(24)
     J = np.triu(rng.normal(size=(n, n)) / np.sqrt(n), 1)
@@ -926,23 +932,84 @@ def run_reference_ais(args, w, rank, world):
     return 0
 
 
+def workload_config(name, w, n, R, Rd):
+    """`config` of a single-instance workload's line; both arms print the
+    same dict so that their lines describe the same job."""
+    return {"workload": name, "n": n, "replicas": R, "reads": Rd,
+            "chains": Rd * R, "update": w["update"],
+            "exchange": "every sweep", "problem": w["kind"],
+            "l2": "GPU arm: flushed (256 MB write) before every timed call "
+                  "(a call is one sweep and its exchange, or a fused launch "
+                  "of up to 128 sweeps whose fields stay in tensor memory); "
+                  "reference arm: host cores, no flush"}
+
+
 def run_reference_arm(args, w, rank, world):
+    """The reference's algorithm on the host cores (the oracle's tuned
+    build, all threads over chains), on real chains of the workload: a step
+    is `per_step` sweeps of `reads` reads (all the workload's reads when one
+    sweep of them takes at most about a second), state carried from step to
+    step as pysa/simulation.py:150-171 carries it, so no step repeats the
+    set-up of its predecessor.  Sized from the warm-up steps so that a step
+    takes about a second."""
     if rank != 0:
         return 0
     if w["kind"] == "ais":
         return run_reference_ais(args, w, rank, world)
+    oracle = _timed_oracle()
+    name = args.workload
+    single = w["kind"] in ("qubo", "sk", "wishart")
     ptype, P, w, what = _reference_sample(w)
     cores = os.cpu_count() or 1
-    reads = 4  # bounded sample: 4 reads x all replicas x 1 sweep per step
-    for _ in range(args.warmup):
-        cpu_reference(w, ptype, P, reads, 1)
-    rates, times = [], []
-    for _ in range(args.steps):
-        r, dt = cpu_reference(w, ptype, P, reads, 1)
-        rates.append(r)
-        times.append(dt)
-    total_attempts = reads * w["replicas"] * w["n"] * args.steps
-    value = total_attempts / sum(times)
+    h = np.diag(P).astype(np.float32).copy()
+    J = P.copy()
+    np.fill_diagonal(J, 0)
+    R, n, Rd = w["replicas"], w["n"], w["reads"]
+    betas = ladder(w)
+
+    def chains(reads):
+        """Seeded random states and their energies s.(J s / 2 + h)."""
+        rng = np.random.default_rng(5)
+        x = rng.integers(0, 2, (reads, R, n)).astype(np.float32)
+        if ptype != "qubo":
+            x = 2 * x - 1
+        x64 = x.reshape(-1, n).astype(np.float64)
+        e = (x64 * (0.5 * (x64 @ J.astype(np.float64)) + h)).sum(1)
+        return x, e.reshape(reads, R).astype(np.float32)
+
+    # calibration: one sweep of 4 reads
+    x, _ = chains(4)
+    t0 = time.perf_counter()
+    oracle.pt_run(ptype, J, h, betas, x, np.zeros((4, R), np.float32),
+                  np.tile(np.arange(R, dtype=np.int32), (4, 1)), seed=1,
+                  num_sweeps=1, update=w["update"])
+    per_read = (time.perf_counter() - t0) / 4
+    # all the workload's reads unless one sweep of them would take over
+    # about 3 s (4 reads overestimate the per-read time: few chains per
+    # thread); sweeps per step rescaled after every warm-up step
+    reads = int(min(Rd, max(4, 3.0 // max(per_read, 1e-9))))
+    per_step = 1
+    x, e = chains(reads)
+    st = dict(spins=x, energies=e,
+              beta_idx=np.tile(np.arange(R, dtype=np.int32), (reads, 1)))
+    best = None
+    times = []
+    sweep = 0
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        out = oracle.pt_run(ptype, J, h, betas, st["spins"], st["energies"],
+                            st["beta_idx"], seed=1, num_sweeps=per_step,
+                            first_sweep=sweep, update=w["update"], best=best)
+        dt = time.perf_counter() - t0
+        sweep += per_step
+        st = out
+        best = (out["best_energy"], out["best_sweep"], out["best_spins"])
+        if k < args.warmup:
+            per_step = int(max(1, round(per_step / max(dt, 1e-9))))
+        if k >= args.warmup:
+            times.append(dt)
+    attempts_per_step = reads * R * n * per_step
+    value = attempts_per_step * len(times) / sum(times)
     line = {
         "impl": "reference", "metric": "spin_flip_attempts_per_s",
         "value": value, "unit": "attempts/s", "n_gpus": world,
@@ -950,14 +1017,18 @@ def run_reference_arm(args, w, rank, world):
         "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, **{k: w[k] for k in w}},
+        "config": (workload_config(name, w, n, R, Rd)
+                   if single else
+                   {"workload": name, **{k: w[k] for k in w}}),
         "cpu_baseline": {
             "value": value, "unit": "attempts/s", "cores": cores,
             "kind": "port",
-            "sample": f"{what}: {reads} reads x {w['replicas']} replicas x "
-                      "1 sweep per step; C restatement of the reference's "
-                      "dense-dot rule, OpenMP over chains (numba not "
-                      "available)"},
+            "sample": f"{what}: {reads} of {Rd} reads x {R} replicas, "
+                      f"{per_step} sweeps (each with its exchange) per timed "
+                      f"step, chains carried across steps; the oracle's "
+                      "C restatement of the reference's dense-dot rule in its "
+                      "build tuned for this CPU, OpenMP over chains (numba is "
+                      "not installed)"},
         "e2e": {"value": value, "unit": "attempts/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -1259,10 +1330,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "n": n, "replicas": R,
-                       "reads": Rd, "chains": C, "update": w["update"],
-                       "exchange": "every sweep", "problem": w["kind"],
-                       "l2": ("flushed (256 MB write) before every timed "
+            "config": workload_config(args.workload, w, n, R, Rd),
+            "timing": {"l2": ("flushed (256 MB write) before every timed "
                               "call of up to %d sweeps; fields stay in "
                               "tensor memory within a launch" % chunk)
                              if fused else

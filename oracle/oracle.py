@@ -28,18 +28,34 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+# the same source built tuned for the host CPU (oracle/Makefile); only the
+# timed CPU-baseline legs select it, the tests use the parity build
+_TIMED_PATH = os.path.join(_HERE, "_build", "liboracle_timed.so")
 _lib = None
+_libs: dict = {}
+_variant = "parity"
 
 TAG_SWEEP, TAG_PT, TAG_PERM, TAG_AIS = 0, 1, 2, 3
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc, no GPU needed)."""
-    if force or not os.path.exists(_LIB_PATH) or (
-            os.path.getmtime(_LIB_PATH) < os.path.getmtime(
-                os.path.join(_HERE, "pt_oracle.c"))):
+    """Compile the oracle with its Makefile (gcc, no GPU needed); returns
+    the path of the selected build (see use_build)."""
+    src = os.path.getmtime(os.path.join(_HERE, "pt_oracle.c"))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src
+                    for p in (_LIB_PATH, _TIMED_PATH)):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
-    return _LIB_PATH
+    return _TIMED_PATH if _variant == "timed" else _LIB_PATH
+
+
+def use_build(variant: str) -> None:
+    """'parity' (default; generic target) or 'timed' (tuned for the host
+    CPU, same arithmetic): the build every later call goes to."""
+    global _variant, _lib
+    if variant not in ("parity", "timed"):
+        raise ValueError(variant)
+    _variant = variant
+    _lib = _libs.get(variant)
 
 
 class _PtArgs(ctypes.Structure):
@@ -82,7 +98,7 @@ class _AisArgs(ctypes.Structure):
 def lib():
     global _lib
     if _lib is None:
-        _lib = ctypes.CDLL(build())
+        _lib = _libs[_variant] = ctypes.CDLL(build())
         P = ctypes.c_void_p
         _lib.orc_philox.argtypes = [P, P, P]
         _lib.orc_draw.argtypes = [ctypes.c_uint64] + [ctypes.c_uint32] * 5
