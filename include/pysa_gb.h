@@ -270,6 +270,16 @@ int pysa_gb_set_trace(void *device_buffer);
  * the call, process-wide.  No counterpart in the reference. */
 int pysa_gb_set_unit_wait_limit(uint64_t ns);
 
+/* Decision mode of the tensor-core sweep's 64-spin blocks: 0 (default)
+ * chooses per block -- rounds over the whole block while the previous
+ * block's largest flip count of a chain was small, sequential 16-spin
+ * sub-blocks otherwise; 1 always rounds; 2 always sub-blocks.  Every mode
+ * makes the same decisions (the rule of pysa/ising.py:40-63 and
+ * pysa/qubo.py:40-63 in the visiting order); only the speed differs, and
+ * tests pin both forms.  Applies to launches enqueued after the call,
+ * process-wide.  No counterpart in the reference. */
+int pysa_gb_set_decision_mode(int32_t mode);
+
 /* Workspace sizing and set-up.
  *   pysa_gb_workspace_bytes: sizes of the workspace arrays for a batch
  *     described by host tables (n, replicas, reads are read); returns the

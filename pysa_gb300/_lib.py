@@ -109,6 +109,7 @@ def load() -> ctypes.CDLL:
         "pysa_gb_abi_version": ([], ctypes.c_int),
         "pysa_gb_set_trace": ([P], ctypes.c_int),
         "pysa_gb_set_unit_wait_limit": ([U64], ctypes.c_int),
+        "pysa_gb_set_decision_mode": ([ctypes.c_int32], ctypes.c_int),
         "pysa_gb_last_error": ([], ctypes.c_char_p),
         "pysa_gb_workspace_bytes": ([I32, P, P], ctypes.c_int),
         "pysa_gb_setup": ([P, P, P, P], ctypes.c_int),

@@ -52,6 +52,7 @@ PlainItemPlan make_item_plan() {
 static thread_local std::string g_last_error;
 static unsigned long long* g_tc_trace = nullptr;  // diagnostics, see below
 static uint64_t g_unit_wait_ns = 0;  // diagnostics: 0 = the default bound
+static int32_t g_decision_mode = 0;   // tensor-core sweep: 0 auto, 1, 2
 
 static int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -133,6 +134,13 @@ int pysa_gb_abi_version(void) { return PYSA_GB_ABI_VERSION; }
 
 int pysa_gb_set_unit_wait_limit(uint64_t ns) {
   g_unit_wait_ns = ns;
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_set_decision_mode(int32_t mode) {
+  if (mode < 0 || mode > 2)
+    return fail(PYSA_GB_ERR_ARG, "decision mode must be 0, 1 or 2");
+  g_decision_mode = mode;
   return PYSA_GB_OK;
 }
 
@@ -632,6 +640,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.use_pt = o->use_pt;
   ta.exchange_every = o->exchange_every;
   ta.unit_wait_ns = g_unit_wait_ns;
+  ta.decision_mode = g_decision_mode;
   ta.sched = ws->tc_sched;
   ta.perm = ws->perm;
   ta.perm_slots = a.perm_slots;

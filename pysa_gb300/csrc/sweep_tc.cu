@@ -34,6 +34,12 @@
 
 namespace pysa_gb {
 
+// Decision mode of a block: block rounds (D64) while the previous block's
+// largest flip count of any chain was at most this, else sequential
+// sub-blocks.  A round costs about as much as 6-10 sequential spins, so the
+// rounds win while flips are rare.
+constexpr uint32_t kD64MaxFlips = 12;
+
 // RND: random visiting order (one permutation per instance and sweep); the
 // B ring keeps two stages to make room for the gathered block fields.
 template <int F, bool RND = false>
@@ -58,8 +64,13 @@ struct TcCfg {
   static constexpr size_t B_STAGE = 32768;
   static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
   static constexpr size_t SPIN_OFF = JBB_OFF + 2 * 16384;
+  // log-uniforms of a block: two buffers of [chain][64] floats in the
+  // swizzled order of cidx() (16-byte stores and loads without bank
+  // conflicts)
   static constexpr size_t LF_OFF = SPIN_OFF + (size_t)CC * WORDS * 4;
   static constexpr size_t DL_OFF = LF_OFF + (size_t)2 * 64 * CC * 4;
+  // deltas [64][CC] (sequential sub-blocks) or the block's loaded fields
+  // [chain][64] swizzled (block rounds)
   static constexpr size_t DE_OFF = DL_OFF + (size_t)64 * CC * 4;
   static constexpr size_t E0_OFF = DE_OFF + (size_t)CC * 8;
   static constexpr size_t EPART_OFF = E0_OFF + (size_t)CC * 8;
@@ -83,19 +94,30 @@ struct TcCfg {
   // by the log-uniform helper warps
   static constexpr size_t POSB_OFF = PERM_OFF + PERM_BYTES;
   static constexpr size_t POSB_BYTES = RND ? (size_t)2 * 2 * CC * 4 : 0;
-  static constexpr size_t BAR_OFF = (POSB_OFF + POSB_BYTES + 63) / 64 * 64;
+  // sequential order, F > 1: the FP32 couplings from the block's spins to
+  // the next block's positions ([64][64], row = flipped spin), with which
+  // the block-round deciders bring the next block's fields up to date
+  // themselves instead of waiting for the tensor cores
+  static constexpr bool PREP = false;
+  static constexpr size_t OFF_OFF = (POSB_OFF + POSB_BYTES + 15) / 16 * 16;
+  static constexpr size_t OFF_BYTES = PREP ? 16384 : 0;
+  static constexpr size_t BAR_OFF = (OFF_OFF + OFF_BYTES + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
-  // lf_full[2], lf_free[2], full[NS], free[NS], drain, mma_done_b[2]
-  static constexpr int NBARS = 16 + 2 * NS;
+  // lf_full[2], lf_free[2], full[NS], free[NS], drain, mma_done_b[2],
+  // off_full, off_free
+  static constexpr int NBARS = 18 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
-  // tmem slot, abort flag, current unit
-  static constexpr size_t BYTES = MISC_OFF + 24;
+  // tmem slot, abort flag, current unit, then per block parity and decision
+  // warp the block's largest flip count of a chain ([2][4] int32)
+  static constexpr size_t STAT_OFF = MISC_OFF + 24;
+  static constexpr size_t BYTES = STAT_OFF + 32;
   static_assert(BYTES <= 232448, "shared memory budget");
 };
 
 struct TcShared {
   uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *rc_full,
-      *rc_done, *lf_full, *lf_free, *full, *free_, *drain, *mma_done_b;
+      *rc_done, *lf_full, *lf_free, *full, *free_, *drain, *mma_done_b,
+      *off_full, *off_free;
   uint32_t* tmem_slot;
   volatile int32_t* abort;
 };
@@ -163,6 +185,15 @@ __device__ __forceinline__ void stamp(const TcArgs& a, uint32_t G, int slot) {
     a.trace[G * 24 + slot] = clock64();
 #endif
 }
+// Trace builds: counters of CTA 0 in row 48, slots 8 + i (i = 0: blocks
+// decided in rounds, 1: in sequential sub-blocks, 2: rounds).
+__device__ __forceinline__ void count(const TcArgs& a, int i, long long v) {
+#ifdef PYSA_GB_TRACE
+  if (a.trace && blockIdx.x == 0)
+    atomicAdd(reinterpret_cast<unsigned long long*>(a.trace + 48 * 24 + 8 + i),
+              (unsigned long long)v);
+#endif
+}
 __device__ __forceinline__ void stamp_cta(const TcArgs& a, int slot) {
 #ifdef PYSA_GB_TRACE
   if (a.trace && blockIdx.x == 0) a.trace[48 * 24 + slot] = clock64();
@@ -198,6 +229,13 @@ __device__ __forceinline__ void named_sync_helpers() {
   asm volatile("barrier.sync 2, 64;" ::: "memory");
 }
 
+// Index of value k (< 64) of chain c in a [chain][64] array whose 16-byte
+// chunks are XOR-swizzled by c % 8: a quarter-warp's 16-byte accesses to the
+// same chunk of 8 consecutive chains land on 8 distinct bank groups.
+__device__ __forceinline__ int cidx(int c, int k) {
+  return c * 64 + ((((k >> 2) ^ (c & 7)) << 2) | (k & 3));
+}
+
 __device__ __forceinline__ uint32_t bf16_bits(float d) {
   // exact for d in {0, +-1, +-2}
   return __float_as_uint(d) >> 16;
@@ -215,7 +253,7 @@ struct RedoCtx {
   const float* corr_s;      // helper corrections (fold 2)
   const float* hbuf;        // gathered fields (random order, fold > 1)
   const int32_t* perm_w;    // this warp's visiting positions (random order)
-  const float* lfb;         // log-uniforms [64][CC]
+  const float* lfb;         // log-uniforms [chain][64], cidx() order
   uint32_t taddr;           // TMEM address of the thread's lane
   int co, kmax, c, g, i0, sb;
   int valid, ising;
@@ -277,7 +315,7 @@ __device__ __noinline__ void redo_subblock(const RedoCtx& x, uint32_t* wcur,
     const float dn =
         x.ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
     const bool acc = x.valid && k < x.kmax &&
-                     metropolis_accept_lf(dn, x.beta, x.lfb[k * CC + c],
+                     metropolis_accept_lf(dn, x.beta, x.lfb[cidx(c, k)],
                                           x.seed, x.inst, x.sweep,
                                           x.chain_local, (uint32_t)(x.i0 + k));
     const float dl =
@@ -331,16 +369,21 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   sh.drain = bars + 13 + 2 * C::NS;
   sh.mma_done_b = bars + 14 + 2 * C::NS;  // [2]: MMAs of blocks using A
                                           // buffer 0 / 1 (two buffers)
+  sh.off_full = bars + 16 + 2 * C::NS;    // one phase per block
+  sh.off_free = bars + 17 + 2 * C::NS;
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
   volatile int32_t* unit_s =
       reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 16);
+  volatile uint32_t* stat_s =
+      reinterpret_cast<volatile uint32_t*>(smem + C::STAT_OFF);
   uint32_t* spins_s = reinterpret_cast<uint32_t*>(smem + C::SPIN_OFF);
   double* dE_s = reinterpret_cast<double*>(smem + C::DE_OFF);
   double* e0_s = reinterpret_cast<double*>(smem + C::E0_OFF);
   double* epart_s = reinterpret_cast<double*>(smem + C::EPART_OFF);
   float* beta_s = reinterpret_cast<float*>(smem + C::BETA_OFF);
   const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
+  const float* offb = reinterpret_cast<const float*>(smem + C::OFF_OFF);
   float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
   float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
   float* corr_s = reinterpret_cast<float*>(smem + C::CORR_OFF);
@@ -401,6 +444,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   uint32_t G = 0;   // blocks
   uint32_t RG = 0;  // recompute blocks
   uint32_t u = 0;   // B ring stages (producer and MMA)
+  // decision warps: this block's decision mode (the same in all 128 threads);
+  // sequential until a block shows few flips
+  bool d64 = a.decision_mode == 1;
+  // block rounds: the next block's fields, brought up to date by the
+  // deciding warp at the end of the previous block (prepared = true)
+  float hp[64];
+  bool prepared = false;
 
   for (;;) {
     // ------------------------------------------------------ next unit
@@ -446,6 +496,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     const int words = (n + 31) >> 5;
     const int64_t chain_base = a.p.chain_off[inst];
     const bool valid = warp < 4 && c < item.nchains;
+    // next-block preparation (block rounds): the producer copies rows of the
+    // instance's FP32 couplings with bulk copies, which need 16-byte aligned
+    // rows
+    const bool prep_inst =
+        C::PREP && (a.p.j_off[inst] & 3) == 0 && (a.p.ld[inst] & 3) == 0 &&
+        (reinterpret_cast<uintptr_t>(a.p.J) & 15) == 0;
     const int64_t chain = item.chain0 + c;
     const uint32_t chain_local = (uint32_t)(chain - chain_base);
     const uint32_t G0 = G, RG0 = RG;
@@ -460,8 +516,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     // block issued in it (for the drain after an abort)
     const uint32_t u_first = u;
     uint32_t jbb_last = 0xFFFFFFFFu;
+    uint32_t off_last = 0xFFFFFFFFu;
 
     // ------------------------------------------------ unit prologue
+    prepared = false;
     for (int i = threadIdx.x; i < CC * C::WORDS; i += blockDim.x) {
       const int w = i / CC, cc = i % CC;  // layout [word][chain]
       spins_s[i] = (cc < item.nchains && w < words)
@@ -698,10 +756,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             }
             named_sync_128();
           }
+          uint32_t blk_mf = 0u;  // largest flip count of a chain (deciders)
+          bool next_prepared = false;
+          {
           bool go = q == qt && !*sh.abort;
           // fields of this block: the previous block's critical MMA (not
           // needed for a unit's first block or after a recompute)
-          if (go && wait_h && !(RND && F > 1))
+          if (go && wait_h && !(RND && F > 1) && !(C::PREP && d64 && prepared))
             go = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
           if (go) go = tc_wait(&sh.jbb_full[Gb & 1], (Gb >> 1) & 1, sh, status);
           if (go) go = tc_wait(&sh.lf_full[Gb & 1], (Gb >> 1) & 1, sh, status);
@@ -774,6 +835,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) dprev[j] = 0.0f;
             bool a_early = false;
+            // bit k: position k of the block flipped (chains the CTA holds,
+            // positions < kmax)
+            uint64_t bflips = 0ull;
             // fields of sub-block g with the corrections of every earlier
             // sub-block of the block
             auto fields = [&](int g, float* hs) {
@@ -839,6 +903,223 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 }
               }
             };
+            // mode-dependent decisions: rounds over the whole block (few
+            // flips) or four sequential sub-blocks of 16 spins
+            uint64_t flips64 = 0ull;
+            if (d64) {
+              // ---------------------------------------- block rounds (D64)
+              // The block's 64 fields in registers.  A round tests every
+              // undecided position against the current fields at once: the
+              // first one not certainly rejected (x >= tl) is the next
+              // decision -- the positions before it are rejected exactly as
+              // the sequential rule rejects them, their fields having seen
+              // every earlier flip.  An accepted flip corrects all 64 fields
+              // (row js of the diagonal block), and the next round starts
+              // after it.  A lane's rounds = its examined candidates + 1;
+              // with few flips per block this replaces 64 dependent
+              // decisions by a handful of wide ones.
+              float* h = hp;
+              if constexpr (!RND) {
+                if (!(C::PREP && prepared))
+                  tc::tmem_ld64(taddr + lane_base + co, h);
+              } else if constexpr (F > 1) {
+#pragma unroll
+                for (int k = 0; k < 64; ++k)
+                  h[k] = k < kmax ? hbuf[k * CC + c] : 0.0f;
+              } else {
+                uint32_t r[16];
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+#pragma unroll
+                  for (int j = 0; j < 16; ++j) {
+                    const int sp = spos(16 * g + j);
+                    r[j] = 0u;
+                    if (sp >= 0)
+                      r[j] = tc::tmem_ld1_nowait(taddr + lane_base + (uint32_t)sp);
+                  }
+                  tc::tmem_wait_ld16(r);
+#pragma unroll
+                  for (int j = 0; j < 16; ++j) h[16 * g + j] = __uint_as_float(r[j]);
+                }
+              }
+              if (lead) stamp(a, Gb, 8);
+              // the block's fields as loaded (a candidate's field at its
+              // decision is rebuilt from them, bit for bit), and per position
+              // w = sigma |tl|: sign = the spin (+ for s = 1), magnitude the
+              // rejection threshold; x >= tl  <=>  (h + w) w >= 0 (exact: a
+              // rounded sum or product keeps the sign of the exact one; an
+              // underflowing product of opposite signs is -0, still < 0)
+#pragma unroll
+              for (int q4 = 0; q4 < 16; ++q4)
+                *reinterpret_cast<float4*>(dl_s + cidx(c, 4 * q4)) =
+                    make_float4(h[4 * q4], h[4 * q4 + 1], h[4 * q4 + 2],
+                                h[4 * q4 + 3]);
+              float w[64];
+#pragma unroll
+              for (int k = 0; k < 64; ++k) {
+                const float lfk = lfb[cidx(c, k)];
+                const float tl = lfk * invbs - fmaf(band1, fabsf(lfk), band0);
+                const uint32_t neg =
+                    ((k < 32 ? ~o0 >> k : ~o1 >> (k - 32)) & 1u) << 31;
+                w[k] = __uint_as_float((__float_as_uint(tl) & 0x7fffffffu) | neg);
+              }
+              const uint64_t live64 =
+                  kmax >= 64 ? ~0ull : ((1ull << kmax) - 1ull);
+              uint64_t pend = valid ? live64 : 0ull;  // undecided positions
+              if (lead) stamp(a, Gb, 9);
+    #pragma unroll 1
+              for (;;) {
+                // first undecided position over the warp: groups of 8
+                // below it are decided in every lane and skipped
+                const uint32_t lo = __reduce_min_sync(
+                    0xffffffffu,
+                    pend ? (uint32_t)(__ffsll((long long)pend) - 1) : 64u);
+                // bit k: position k certainly rejected (x < tl)
+                uint32_t m[8];
+#pragma unroll
+                for (int qd = 0; qd < 8; ++qd) {
+                  m[qd] = 0u;
+                  if (8 * qd + 8 > (int)lo) {
+#pragma unroll
+                    for (int jj = 7; jj >= 0; --jj) {
+                      const int k = 8 * qd + jj;
+                      // (h + w) w < 0: the signs differ (a zero sum counts
+                      // as rejected: x = tl exactly, safely below the band)
+                      const uint32_t x = __float_as_uint((h[k] + w[k]) * w[k]);
+                      m[qd] = __funnelshift_l(x, m[qd], 1);
+                    }
+                  }
+                }
+                const uint32_t e0 =
+                    m[0] | (m[1] << 8) | (m[2] << 16) | (m[3] << 24);
+                const uint32_t e1 =
+                    m[4] | (m[5] << 8) | (m[6] << 16) | (m[7] << 24);
+                const uint64_t cand =
+                    ~(((uint64_t)e1 << 32) | (uint64_t)e0) & pend;
+                if (lead) count(a, 2, 1);
+                if (__all_sync(0xffffffffu, cand == 0ull)) break;
+                if (cand == 0ull) pend = 0ull;  // the rest rejected: done
+                if (cand != 0ull) {
+                  const int js = __ffsll((long long)cand) - 1;
+                  const uint64_t bit = 1ull << js;
+                  pend &= ~((bit << 1) - 1ull);  // positions <= js decided
+                  // the field at decision: loaded value + this block's
+                  // earlier flips, in the order the registers took them
+                  float hj = dl_s[cidx(c, js)];
+                  uint64_t fb = flips64;
+                  while (fb) {
+                    const int i = __ffsll((long long)fb) - 1;
+                    fb &= fb - 1ull;
+                    const uint32_t si = (i < 32 ? o0 >> i : o1 >> (i - 32)) & 1u;
+                    hj = fmaf(si ? -scale : scale, jb[i * 64 + js], hj);
+                  }
+                  const bool sbit =
+                      ((js < 32 ? o0 >> js : o1 >> (js - 32)) & 1u) != 0u;
+                  const float x = sbit ? hj : -hj;
+                  const float lfk = lfb[cidx(c, js)];
+                  const float th = fminf(
+                      fmaf(lfk, invbs, fmaf(band1, fabsf(lfk), band0)), 0.0f);
+                  bool acc = x >= th;
+                  if (!acc) {
+                    // inside the band: the exact rule
+                    acc = metropolis_accept_lf(
+                        scale * x, beta, lfk,
+                        chain_seed(a.seed, a.s.stream_key, chain),
+                        (uint32_t)inst, sweep, chain_local, (uint32_t)(i0 + js));
+                  }
+                  if (acc) {
+                    flips64 |= bit;
+                    const float dl = sbit ? -scale : scale;
+                    dEb = fmaf(dl, hj, dEb);  // dl h = -dn
+                    const float4* row =
+                        reinterpret_cast<const float4*>(jb + js * 64);
+#pragma unroll
+                    for (int q4 = 0; q4 < 16; ++q4) {
+                      const float4 v = row[q4];
+                      h[4 * q4 + 0] = fmaf(dl, v.x, h[4 * q4 + 0]);
+                      h[4 * q4 + 1] = fmaf(dl, v.y, h[4 * q4 + 1]);
+                      h[4 * q4 + 2] = fmaf(dl, v.z, h[4 * q4 + 2]);
+                      h[4 * q4 + 3] = fmaf(dl, v.w, h[4 * q4 + 3]);
+                    }
+                  }
+                }
+              }
+              w0 = o0 ^ (uint32_t)flips64;
+              w1 = o1 ^ (uint32_t)(flips64 >> 32);
+              if (lead) stamp(a, Gb, 10);
+              // the next block's fields, when this warp decides it too and
+              // nothing rebuilds them first: tensor memory as of the
+              // previous block's MMAs (all done) plus this block's flips,
+              // applied here with the FP32 couplings to the next block's
+              // positions -- the next block then needs no MMA to start
+              bool prep_next = false;
+              if constexpr (C::PREP) {
+                const int tn = t + 1 < NB ? t + 1 : 0;
+                prep_next = Gb + 1 < Gend && (64 * tn) / S == qt &&
+                            !(tn == 0 && rc_at(s + 1)) && prep_inst;
+                if (prep_next) {
+                  // (two A buffers: the per-block barrier may lag two
+                  // phases, so the per-buffer ones are waited)
+                  bool pok = Gb == G0 ||
+                             mmas_done_through<C::A_NBUF>(Gb - 1, sh, status);
+                  if (pok) pok = tc_wait(sh.off_full, Gb & 1, sh, status);
+                  pok = __all_sync(0xffffffffu, pok);
+                  if (pok) {
+                    tc::fence_after_sync();
+                    tc::tmem_ld64(taddr + lane_base + (64 * tn) % S, h);
+                    uint64_t fb = flips64;
+                    while (fb) {
+                      const int i = __ffsll((long long)fb) - 1;
+                      fb &= fb - 1ull;
+                      const float dl =
+                          ((i < 32 ? o0 >> i : o1 >> (i - 32)) & 1u) ? -scale
+                                                                     : scale;
+                      const float4* row =
+                          reinterpret_cast<const float4*>(offb + i * 64);
+#pragma unroll
+                      for (int q4 = 0; q4 < 16; ++q4) {
+                        const float4 v = row[q4];
+                        h[4 * q4 + 0] = fmaf(dl, v.x, h[4 * q4 + 0]);
+                        h[4 * q4 + 1] = fmaf(dl, v.y, h[4 * q4 + 1]);
+                        h[4 * q4 + 2] = fmaf(dl, v.z, h[4 * q4 + 2]);
+                        h[4 * q4 + 3] = fmaf(dl, v.w, h[4 * q4 + 3]);
+                      }
+                    }
+                  }
+                  prep_next = pok;
+                }
+              }
+              next_prepared = prep_next;
+              // A row: zeros, then the flipped positions' deltas, once the
+              // MMAs reading this A buffer have completed
+              bool a_ok = true;
+              if constexpr (C::A_NBUF == 2) {
+                a_ok = a_buffer_free();
+              } else {
+                if (Gb > G0) a_ok = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
+              }
+              if (lead) stamp(a, Gb, 11);
+              if (a_ok) {
+                const int m = 128 - CC + c +
+                              (C::A_NBUF == 2 ? 128 * (int)(Gb & 1) : 0);
+                unsigned char* rowp = smem + C::A_OFF + ((m >> 3) * 8) * 128 +
+                                      (m & 7) * 16;
+#pragma unroll
+                for (int kc = 0; kc < 8; ++kc)
+                  *reinterpret_cast<uint4*>(rowp + kc * 128) =
+                      make_uint4(0u, 0u, 0u, 0u);
+                const uint16_t one = ising ? 0x4000u : 0x3F80u;  // BF16 scale
+                uint64_t fb = flips64;
+                while (fb) {
+                  const int j = __ffsll((long long)fb) - 1;
+                  fb &= fb - 1ull;
+                  const uint32_t sj = (j < 32 ? o0 >> j : o1 >> (j - 32)) & 1u;
+                  *reinterpret_cast<uint16_t*>(rowp + (j >> 3) * 128 +
+                                               (j & 7) * 2) =
+                      (uint16_t)(one | (sj ? 0x8000u : 0u));
+                }
+              }
+            } else {
             // four sub-blocks of 16 spins
     #pragma unroll 1
             for (int g = 0; g < 4; ++g) {
@@ -854,7 +1135,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   nlive >= 16 ? 0xFFFFu : nlive > 0 ? (1u << nlive) - 1u : 0u;
               float lfv[16];
 #pragma unroll
-              for (int j = 0; j < 16; ++j) lfv[j] = lfb[(16 * g + j) * CC + c];
+              for (int j = 0; j < 16; ++j) lfv[j] = lfb[cidx(c, 16 * g + j)];
 
               // fast pass: branch-free decisions on the thresholds; a
               // decision inside the band is only flagged here.  No shared
@@ -929,6 +1210,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 for (int j = 0; j < 16; ++j) dcur[j] = dl_s[(16 * g + j) * CC + c];
               }
               if (g < 2) w0 = wcur; else w1 = wcur;
+              // this sub-block's flips (chains the CTA holds)
+              bflips |= (uint64_t)(valid ? ((wcur ^ wsave) >> sb) & 0xFFFFu : 0u)
+                        << (16 * g);
 #pragma unroll
               for (int j = 0; j < 16; ++j) dl_s[(16 * g + j) * CC + c] = dcur[j];
               // deltas into the A rows.  A is single-buffered: the previous
@@ -978,6 +1262,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 }
               }
             }
+            flips64 = bflips;
+            }  // sequential sub-blocks
             if (valid) {
               if constexpr (!RND) {
                 spins_s[(2 * t) * CC + c] = w0;
@@ -1000,8 +1286,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
               dE_s[c] += (double)dEb;
             }
+            blk_mf = __reduce_max_sync(
+                0xffffffffu, valid ? (uint32_t)__popcll(flips64) : 0u);
+            if (lead) count(a, d64 ? 0 : 1, 1);
             fence_proxy_async();
-          } else if constexpr (C::APUT) {
+          } else if (C::APUT && !d64) {
             // one of the three other slices' warps (or every warp after an
             // abort): the A rows of sub-block hr once sub-blocks 0-2 are
             // decided and the previous block's MMAs are done
@@ -1015,7 +1304,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               put_a(hr, d);
             }
             fence_proxy_async();
-          } else if (C::HELP) {
+          } else if (C::HELP && !d64) {
             // helper (the other slice's thread of chain c), or a deciding
             // thread after an abort: same three barriers as the deciding path
             const bool hgo = __all_sync(0xffffffffu, !*sh.abort) && q != qt;
@@ -1093,13 +1382,26 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             put_decided(3, true);
             fence_proxy_async();
           }
-          if (lane == 0) stamp(a, Gb, 20 + warp);
+          }
+          prepared = next_prepared;
+          if (lane == 0) {
+            stamp(a, Gb, 20 + warp);
+            stat_s[(Gb & 1) * 4 + warp] = blk_mf;
+          }
           named_sync_128();
+          {
+            uint32_t mf = 0u;
+#pragma unroll
+            for (int w4 = 0; w4 < 4; ++w4) mf = max(mf, stat_s[(Gb & 1) * 4 + w4]);
+            d64 = a.decision_mode == 1 ||
+                  (a.decision_mode == 0 && mf <= kD64MaxFlips);
+          }
           if (threadIdx.x == 0) {
             stamp(a, Gb, 4);
             mbar_arrive(sh.a_full);
             mbar_arrive(&sh.jbb_free[Gb & 1]);
             mbar_arrive(&sh.lf_free[Gb & 1]);
+            if (C::PREP) mbar_arrive(sh.off_free);
           }
         }  // blocks
 
@@ -1405,6 +1707,30 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           if (r) jbb_last = Gx;
           return r;
         };
+        // block Gx's couplings to the next block's positions (rows of the
+        // transposed FP32 couplings, next block's columns) into OFF, once
+        // block Gx - 1 is done with it; one phase of off_full per block (an
+        // empty one when the rows are not 16-byte aligned)
+        auto issue_off = [&](uint32_t Gx, int tx) {
+          if (Gx >= 1 && !tc_wait(sh.off_free, (Gx - 1) & 1, sh, status))
+            return false;
+          const int tn = tx + 1 < NB ? tx + 1 : 0;
+          const int kt = n - 64 * tx < 64 ? n - 64 * tx : 64;
+          const int kn = n - 64 * tn < 64 ? n - 64 * tn : 64;
+          const uint32_t row_bytes = (uint32_t)((kn + 3) & ~3) * 4u;
+          mbar_expect_tx_arrive(sh.off_full,
+                                prep_inst ? (uint32_t)kt * row_bytes : 0u);
+          if (prep_inst) {
+            const int ld = a.p.ld[inst];
+            const float* Jt = a.p.J + a.p.j_off[inst];
+            for (int i = 0; i < kt; ++i)
+              bulk_g2s(smem + C::OFF_OFF + (size_t)i * 256,
+                       Jt + (int64_t)(64 * tx + i) * ld + 64 * tn, row_bytes,
+                       sh.off_full);
+          }
+          off_last = Gx;
+          return true;
+        };
         bool ok = issue_jbb_t(G0);
         for (int s = 0; s < KU && ok; ++s) {
           if (rc_at(s)) {
@@ -1421,6 +1747,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
             // the next block's diagonal block lands while this one is decided
             if (Gb + 1 < Gend) ok = issue_jbb_t(Gb + 1);
+            if (C::PREP && ok) ok = issue_off(Gb, t);
             const bool has_next = Gb + 1 < Gend;
             const int tn = (t + 1) % NB;
             const int jf = has_next ? ((64 * tn) % S) / 256 : 0;
@@ -1458,9 +1785,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               uint32_t x[4];
               draw4(sk, TAG_SWEEP, (uint32_t)inst, sweep, cl,
                     (uint32_t)(16 * t + quad), x);
-#pragma unroll
-              for (int e = 0; e < 4; ++e)
-                out[(4 * quad + e) * CC + c2] = log_uniform_f32(x[e]);
+              *reinterpret_cast<float4*>(out + cidx(c2, 4 * quad)) =
+                  make_float4(log_uniform_f32(x[0]), log_uniform_f32(x[1]),
+                              log_uniform_f32(x[2]), log_uniform_f32(x[3]));
             }
           }
           if constexpr (RND) {
@@ -1521,6 +1848,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             u - u_first > (uint32_t)C::NS ? u - (uint32_t)C::NS : u_first;
         for (uint32_t x = lo; x < u; ++x)
           drain_wait(&sh.full[x % C::NS], (x / C::NS) & 1);
+        if (off_last != 0xFFFFFFFFu) drain_wait(sh.off_full, off_last & 1);
         if (jbb_last != 0xFFFFFFFFu) {
           drain_wait(&sh.jbb_full[jbb_last & 1], (jbb_last >> 1) & 1);
           if (jbb_last > G0)

@@ -33,6 +33,8 @@ struct TcArgs {
   int32_t advance_counter;  // 1: the last CTA advances the sweep counter
   int32_t exchange_every;   // <= 1: every sweep; k: after (s + 1) % k == 0
   uint64_t unit_wait_ns;  // bound of the wait for an item's previous unit
+  int32_t decision_mode;  // 0 per-block choice, 1 block rounds, 2 sub-blocks
+  int32_t pad_mode_;
                           // (0: one second)
   int32_t* sched;  // zeroed per launch: [0] unit queue, [1] finished CTAs,
                    // [2 + item] units of the item done

@@ -80,6 +80,63 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 lanes x 64 columns: two 32-column loads and one wait whose operands are
+// all 64 registers, so no use of them is scheduled above the wait.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float* v) {
+  uint32_t r[64];
+  __syncwarp();
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t* q = r + 32 * h;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, "
+        "[%32];"
+        : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]), "=r"(q[4]),
+          "=r"(q[5]), "=r"(q[6]), "=r"(q[7]), "=r"(q[8]), "=r"(q[9]),
+          "=r"(q[10]), "=r"(q[11]), "=r"(q[12]), "=r"(q[13]), "=r"(q[14]),
+          "=r"(q[15]), "=r"(q[16]), "=r"(q[17]), "=r"(q[18]), "=r"(q[19]),
+          "=r"(q[20]), "=r"(q[21]), "=r"(q[22]), "=r"(q[23]), "=r"(q[24]),
+          "=r"(q[25]), "=r"(q[26]), "=r"(q[27]), "=r"(q[28]), "=r"(q[29]),
+          "=r"(q[30]), "=r"(q[31])
+        : "r"(taddr + 32u * h)
+        : "memory");
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t* q = r + 32 * h;
+    // the wait is issued once (h == 0); the second statement only pins the
+    // other 32 registers below it
+    if (h == 0)
+      asm volatile(
+          "tcgen05.wait::ld.sync.aligned;"
+          : "+r"(q[0]), "+r"(q[1]), "+r"(q[2]), "+r"(q[3]), "+r"(q[4]),
+            "+r"(q[5]), "+r"(q[6]), "+r"(q[7]), "+r"(q[8]), "+r"(q[9]),
+            "+r"(q[10]), "+r"(q[11]), "+r"(q[12]), "+r"(q[13]), "+r"(q[14]),
+            "+r"(q[15]), "+r"(q[16]), "+r"(q[17]), "+r"(q[18]), "+r"(q[19]),
+            "+r"(q[20]), "+r"(q[21]), "+r"(q[22]), "+r"(q[23]), "+r"(q[24]),
+            "+r"(q[25]), "+r"(q[26]), "+r"(q[27]), "+r"(q[28]), "+r"(q[29]),
+            "+r"(q[30]), "+r"(q[31])
+          :
+          : "memory");
+    else
+      asm volatile(
+          ""
+          : "+r"(q[0]), "+r"(q[1]), "+r"(q[2]), "+r"(q[3]), "+r"(q[4]),
+            "+r"(q[5]), "+r"(q[6]), "+r"(q[7]), "+r"(q[8]), "+r"(q[9]),
+            "+r"(q[10]), "+r"(q[11]), "+r"(q[12]), "+r"(q[13]), "+r"(q[14]),
+            "+r"(q[15]), "+r"(q[16]), "+r"(q[17]), "+r"(q[18]), "+r"(q[19]),
+            "+r"(q[20]), "+r"(q[21]), "+r"(q[22]), "+r"(q[23]), "+r"(q[24]),
+            "+r"(q[25]), "+r"(q[26]), "+r"(q[27]), "+r"(q[28]), "+r"(q[29]),
+            "+r"(q[30]), "+r"(q[31])
+          :
+          : "memory");
+  }
+#pragma unroll
+  for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // Waits for this thread's TMEM loads; the 16 registers of the last one are
 // operands of the wait, so no use of them is scheduled above it.
 __device__ __forceinline__ void tmem_wait_ld16(uint32_t* r) {
