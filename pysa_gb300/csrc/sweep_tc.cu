@@ -34,6 +34,10 @@
 
 namespace pysa_gb {
 
+// B tile width: columns of one tile (one ring stage, one MMA group of N =
+// kTW).
+constexpr int kTW = 256;
+
 // Decision mode of a block: block rounds (D64) while the previous block's
 // largest flip count of any chain was at most this, else sequential
 // sub-blocks.  A round costs about as much as 6-10 sequential spins, so the
@@ -61,7 +65,7 @@ struct TcCfg {
   static constexpr size_t A_OFF = 0;
   static constexpr size_t A_BYTES = (size_t)A_ROWS * 128;
   static constexpr size_t B_OFF = A_OFF + A_BYTES;
-  static constexpr size_t B_STAGE = 32768;
+  static constexpr size_t B_STAGE = (size_t)kTW * 128;  // one tile
   static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
   static constexpr size_t SPIN_OFF = JBB_OFF + 2 * 16384;
   // log-uniforms of a block: two buffers of [chain][64] floats in the
@@ -94,18 +98,10 @@ struct TcCfg {
   // by the log-uniform helper warps
   static constexpr size_t POSB_OFF = PERM_OFF + PERM_BYTES;
   static constexpr size_t POSB_BYTES = RND ? (size_t)2 * 2 * CC * 4 : 0;
-  // sequential order, F > 1: the FP32 couplings from the block's spins to
-  // the next block's positions ([64][64], row = flipped spin), with which
-  // the block-round deciders bring the next block's fields up to date
-  // themselves instead of waiting for the tensor cores
-  static constexpr bool PREP = false;
-  static constexpr size_t OFF_OFF = (POSB_OFF + POSB_BYTES + 15) / 16 * 16;
-  static constexpr size_t OFF_BYTES = PREP ? 16384 : 0;
-  static constexpr size_t BAR_OFF = (OFF_OFF + OFF_BYTES + 63) / 64 * 64;
+  static constexpr size_t BAR_OFF = (POSB_OFF + POSB_BYTES + 63) / 64 * 64;
   // a_full, mma_done, h_ready, jbb_full[2], jbb_free[2], rc_full, rc_done,
-  // lf_full[2], lf_free[2], full[NS], free[NS], drain, mma_done_b[2],
-  // off_full, off_free
-  static constexpr int NBARS = 18 + 2 * NS;
+  // lf_full[2], lf_free[2], full[NS], free[NS], drain, mma_done_b[2]
+  static constexpr int NBARS = 16 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
   // tmem slot, abort flag, current unit, then per block parity and decision
   // warp the block's largest flip count of a chain ([2][4] int32)
@@ -116,8 +112,7 @@ struct TcCfg {
 
 struct TcShared {
   uint64_t *a_full, *mma_done, *h_ready, *jbb_full, *jbb_free, *rc_full,
-      *rc_done, *lf_full, *lf_free, *full, *free_, *drain, *mma_done_b,
-      *off_full, *off_free;
+      *rc_done, *lf_full, *lf_free, *full, *free_, *drain, *mma_done_b;
   uint32_t* tmem_slot;
   volatile int32_t* abort;
 };
@@ -369,8 +364,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   sh.drain = bars + 13 + 2 * C::NS;
   sh.mma_done_b = bars + 14 + 2 * C::NS;  // [2]: MMAs of blocks using A
                                           // buffer 0 / 1 (two buffers)
-  sh.off_full = bars + 16 + 2 * C::NS;    // one phase per block
-  sh.off_free = bars + 17 + 2 * C::NS;
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
   volatile int32_t* unit_s =
@@ -383,7 +376,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   double* epart_s = reinterpret_cast<double*>(smem + C::EPART_OFF);
   float* beta_s = reinterpret_cast<float*>(smem + C::BETA_OFF);
   const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
-  const float* offb = reinterpret_cast<const float*>(smem + C::OFF_OFF);
   float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
   float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
   float* corr_s = reinterpret_cast<float*>(smem + C::CORR_OFF);
@@ -431,7 +423,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *sh.tmem_slot;
-  const uint32_t idesc_full = tc::idesc_bf16(128, 256);
+  const uint32_t idesc_full = tc::idesc_bf16(128, kTW);
 
   // decision-thread identity: TMEM lane L = slice q, chain c
   const int L = threadIdx.x;
@@ -447,10 +439,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   // decision warps: this block's decision mode (the same in all 128 threads);
   // sequential until a block shows few flips
   bool d64 = a.decision_mode == 1;
-  // block rounds: the next block's fields, brought up to date by the
-  // deciding warp at the end of the previous block (prepared = true)
-  float hp[64];
-  bool prepared = false;
 
   for (;;) {
     // ------------------------------------------------------ next unit
@@ -492,16 +480,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
     const int S = NP / F;
     const int NB = (n + 63) / 64;
-    const int NT = (S + 255) / 256;
+    const int NT = (S + kTW - 1) / kTW;
     const int words = (n + 31) >> 5;
     const int64_t chain_base = a.p.chain_off[inst];
     const bool valid = warp < 4 && c < item.nchains;
-    // next-block preparation (block rounds): the producer copies rows of the
-    // instance's FP32 couplings with bulk copies, which need 16-byte aligned
-    // rows
-    const bool prep_inst =
-        C::PREP && (a.p.j_off[inst] & 3) == 0 && (a.p.ld[inst] & 3) == 0 &&
-        (reinterpret_cast<uintptr_t>(a.p.J) & 15) == 0;
     const int64_t chain = item.chain0 + c;
     const uint32_t chain_local = (uint32_t)(chain - chain_base);
     const uint32_t G0 = G, RG0 = RG;
@@ -516,10 +498,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     // block issued in it (for the drain after an abort)
     const uint32_t u_first = u;
     uint32_t jbb_last = 0xFFFFFFFFu;
-    uint32_t off_last = 0xFFFFFFFFu;
 
     // ------------------------------------------------ unit prologue
-    prepared = false;
     for (int i = threadIdx.x; i < CC * C::WORDS; i += blockDim.x) {
       const int w = i / CC, cc = i % CC;  // layout [word][chain]
       spins_s[i] = (cc < item.nchains && w < words)
@@ -757,12 +737,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             named_sync_128();
           }
           uint32_t blk_mf = 0u;  // largest flip count of a chain (deciders)
-          bool next_prepared = false;
           {
           bool go = q == qt && !*sh.abort;
           // fields of this block: the previous block's critical MMA (not
           // needed for a unit's first block or after a recompute)
-          if (go && wait_h && !(RND && F > 1) && !(C::PREP && d64 && prepared))
+          if (go && wait_h && !(RND && F > 1))
             go = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
           if (go) go = tc_wait(&sh.jbb_full[Gb & 1], (Gb >> 1) & 1, sh, status);
           if (go) go = tc_wait(&sh.lf_full[Gb & 1], (Gb >> 1) & 1, sh, status);
@@ -918,10 +897,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               // after it.  A lane's rounds = its examined candidates + 1;
               // with few flips per block this replaces 64 dependent
               // decisions by a handful of wide ones.
-              float* h = hp;
+              float h[64];
               if constexpr (!RND) {
-                if (!(C::PREP && prepared))
-                  tc::tmem_ld64(taddr + lane_base + co, h);
+                tc::tmem_ld64(taddr + lane_base + co, h);
               } else if constexpr (F > 1) {
 #pragma unroll
                 for (int k = 0; k < 64; ++k)
@@ -1047,49 +1025,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               w0 = o0 ^ (uint32_t)flips64;
               w1 = o1 ^ (uint32_t)(flips64 >> 32);
               if (lead) stamp(a, Gb, 10);
-              // the next block's fields, when this warp decides it too and
-              // nothing rebuilds them first: tensor memory as of the
-              // previous block's MMAs (all done) plus this block's flips,
-              // applied here with the FP32 couplings to the next block's
-              // positions -- the next block then needs no MMA to start
-              bool prep_next = false;
-              if constexpr (C::PREP) {
-                const int tn = t + 1 < NB ? t + 1 : 0;
-                prep_next = Gb + 1 < Gend && (64 * tn) / S == qt &&
-                            !(tn == 0 && rc_at(s + 1)) && prep_inst;
-                if (prep_next) {
-                  // (two A buffers: the per-block barrier may lag two
-                  // phases, so the per-buffer ones are waited)
-                  bool pok = Gb == G0 ||
-                             mmas_done_through<C::A_NBUF>(Gb - 1, sh, status);
-                  if (pok) pok = tc_wait(sh.off_full, Gb & 1, sh, status);
-                  pok = __all_sync(0xffffffffu, pok);
-                  if (pok) {
-                    tc::fence_after_sync();
-                    tc::tmem_ld64(taddr + lane_base + (64 * tn) % S, h);
-                    uint64_t fb = flips64;
-                    while (fb) {
-                      const int i = __ffsll((long long)fb) - 1;
-                      fb &= fb - 1ull;
-                      const float dl =
-                          ((i < 32 ? o0 >> i : o1 >> (i - 32)) & 1u) ? -scale
-                                                                     : scale;
-                      const float4* row =
-                          reinterpret_cast<const float4*>(offb + i * 64);
-#pragma unroll
-                      for (int q4 = 0; q4 < 16; ++q4) {
-                        const float4 v = row[q4];
-                        h[4 * q4 + 0] = fmaf(dl, v.x, h[4 * q4 + 0]);
-                        h[4 * q4 + 1] = fmaf(dl, v.y, h[4 * q4 + 1]);
-                        h[4 * q4 + 2] = fmaf(dl, v.z, h[4 * q4 + 2]);
-                        h[4 * q4 + 3] = fmaf(dl, v.w, h[4 * q4 + 3]);
-                      }
-                    }
-                  }
-                  prep_next = pok;
-                }
-              }
-              next_prepared = prep_next;
+
               // A row: zeros, then the flipped positions' deltas, once the
               // MMAs reading this A buffer have completed
               bool a_ok = true;
@@ -1383,7 +1319,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             fence_proxy_async();
           }
           }
-          prepared = next_prepared;
           if (lane == 0) {
             stamp(a, Gb, 20 + warp);
             stat_s[(Gb & 1) * 4 + warp] = blk_mf;
@@ -1401,7 +1336,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             mbar_arrive(sh.a_full);
             mbar_arrive(&sh.jbb_free[Gb & 1]);
             mbar_arrive(&sh.lf_free[Gb & 1]);
-            if (C::PREP) mbar_arrive(sh.off_free);
           }
         }  // blocks
 
@@ -1535,12 +1469,12 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     } else if (warp == 4) {
       // ============================================================== MMA
       if (lane == 0) {
-        // rows [r_lo, r_hi) of the 256-row B tile in `slot` against A slice
-        // qq, into the field columns 256 j + r_lo ...
+        // rows [r_lo, r_hi) of the kTW-row B tile in `slot` against A slice
+        // qq, into the field columns kTW j + r_lo ...
         auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi,
                             uint32_t acc, int ab) {
           if (r_hi <= r_lo) return;
-          const uint32_t idesc = r_hi - r_lo == 256
+          const uint32_t idesc = r_hi - r_lo == kTW
                                      ? idesc_full
                                      : tc::idesc_bf16(128, r_hi - r_lo);
           // slice qq's view: 128 rows starting (128 - CC - qq CC) rows in
@@ -1557,7 +1491,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           const uint64_t bd = tc::smem_desc(b0, 128, 1024);
 #pragma unroll
           for (int ks = 0; ks < 4; ++ks)
-            tc::mma_bf16(taddr + 256 * j + r_lo, ad + 16u * ks, bd + 16u * ks,
+            tc::mma_bf16(taddr + kTW * j + r_lo, ad + 16u * ks, bd + 16u * ks,
                          idesc, (acc | (uint32_t)ks) ? 1u : 0u);
         };
         bool ok = true;
@@ -1570,7 +1504,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
               tc::fence_after_sync();
               for (int j = 0; j < NT && ok; ++j) {
-                const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+                const int width = S - kTW * j < kTW ? S - kTW * j : kTW;
                 for (int term = 0; term < T && ok; ++term) {
                   for (int qq = 0; qq < F; ++qq) {
                     const uint32_t slot = u % C::NS;
@@ -1599,7 +1533,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             const bool has_next = Gb + 1 < Gend;
             const int tn = t + 1 < NB ? t + 1 : 0;
             const int qn = (64 * tn) / S, cn = 64 * tn - qn * S;
-            const int jf = has_next ? cn >> 8 : 0, r0 = cn & 255;
+            const int jf = has_next ? cn / kTW : 0, r0 = cn % kTW;
             asm volatile("" ::"r"(jf), "r"(r0), "r"(qn));
             if (!tc_wait(sh.a_full, Gb & 1, sh, status)) {
               ok = false;
@@ -1608,13 +1542,15 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             stamp(a, Gb, 5);
             tc::fence_after_sync();
             const int ab = C::A_NBUF == 2 ? (int)(Gb & 1) : 0;
-            for (int jj = 0; jj < NT && ok; ++jj) {
-              const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
-              const int width = S - 256 * j < 256 ? S - 256 * j : 256;
-              // stage order: slices from qn on, terms inside (the producer
-              // issues the same order)
-              for (int k = 0; k < F && ok; ++k) {
-                const int qq = (qn + k) % F;
+            // stage order: slices from qn on, tiles inside (the critical
+            // one first), terms innermost -- consecutive stages write
+            // different accumulator tiles, so their MMAs need not wait for
+            // one another (the producer issues the same order)
+            for (int k = 0; k < F && ok; ++k) {
+              const int qq = (qn + k) % F;
+              for (int jj = 0; jj < NT && ok; ++jj) {
+                const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
+                const int width = S - kTW * j < kTW ? S - kTW * j : kTW;
                 // random order: the next block's columns are scattered, so
                 // no tile is critical; h_ready follows the whole block
                 const bool crit = !RND && jj == 0 && k == 0 && has_next;
@@ -1625,6 +1561,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                     ok = false;
                     break;
                   }
+                  if (k * NT + jj < 4 && term == 0) stamp(a, Gb, 12 + k * NT + jj);
                   tc::fence_after_sync();
                   if (crit)
                     mma_rows(slot, qq, j, r0, r0 + 64, 1u, ab);
@@ -1663,7 +1600,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
       if (lane == 0) {
         const uint16_t* Bp = a.tc_b + item.b_off;
         const float* D = a.tc_diag + item.diag_off;
-        const size_t tile_elems = 256 * 64;
+        const size_t tile_elems = (size_t)kTW * 64;
         // diagonal block of global block Gx (block (Gx - G0) % NB of the
         // unit) into buffer Gx & 1, once block Gx - 2 has released it
         // random order: the sweep's repacked slot (same offsets)
@@ -1692,7 +1629,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           if (u >= (uint32_t)C::NS &&
               !tc_wait(&sh.free_[slot], ((u / C::NS) - 1) & 1, sh, status))
             return false;
-          const int width = S - 256 * j < 256 ? S - 256 * j : 256;
+          const int width = S - kTW * j < kTW ? S - kTW * j : kTW;
           const size_t src =
               ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
           const uint32_t bytes = (uint32_t)width * 128;
@@ -1706,30 +1643,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           const bool r = issue_jbb(Gx);
           if (r) jbb_last = Gx;
           return r;
-        };
-        // block Gx's couplings to the next block's positions (rows of the
-        // transposed FP32 couplings, next block's columns) into OFF, once
-        // block Gx - 1 is done with it; one phase of off_full per block (an
-        // empty one when the rows are not 16-byte aligned)
-        auto issue_off = [&](uint32_t Gx, int tx) {
-          if (Gx >= 1 && !tc_wait(sh.off_free, (Gx - 1) & 1, sh, status))
-            return false;
-          const int tn = tx + 1 < NB ? tx + 1 : 0;
-          const int kt = n - 64 * tx < 64 ? n - 64 * tx : 64;
-          const int kn = n - 64 * tn < 64 ? n - 64 * tn : 64;
-          const uint32_t row_bytes = (uint32_t)((kn + 3) & ~3) * 4u;
-          mbar_expect_tx_arrive(sh.off_full,
-                                prep_inst ? (uint32_t)kt * row_bytes : 0u);
-          if (prep_inst) {
-            const int ld = a.p.ld[inst];
-            const float* Jt = a.p.J + a.p.j_off[inst];
-            for (int i = 0; i < kt; ++i)
-              bulk_g2s(smem + C::OFF_OFF + (size_t)i * 256,
-                       Jt + (int64_t)(64 * tx + i) * ld + 64 * tn, row_bytes,
-                       sh.off_full);
-          }
-          off_last = Gx;
-          return true;
         };
         bool ok = issue_jbb_t(G0);
         for (int s = 0; s < KU && ok; ++s) {
@@ -1747,17 +1660,16 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             const uint32_t Gb = G0 + (uint32_t)(s * NB + t);
             // the next block's diagonal block lands while this one is decided
             if (Gb + 1 < Gend) ok = issue_jbb_t(Gb + 1);
-            if (C::PREP && ok) ok = issue_off(Gb, t);
             const bool has_next = Gb + 1 < Gend;
             const int tn = (t + 1) % NB;
-            const int jf = has_next ? ((64 * tn) % S) / 256 : 0;
+            const int jf = has_next ? ((64 * tn) % S) / kTW : 0;
             const int qn = (64 * tn) / S;
-            for (int jj = 0; jj < NT && ok; ++jj) {
-              const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
-              for (int k = 0; k < F && ok; ++k)
+            for (int k = 0; k < F && ok; ++k)
+              for (int jj = 0; jj < NT && ok; ++jj) {
+                const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
                 for (int term = 0; term < T && ok; ++term)
                   ok = issue_stage(Bs, t, term, (qn + k) % F, j);
-            }
+              }
             stamp(a, Gb, 7);
           }
         }
@@ -1848,7 +1760,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             u - u_first > (uint32_t)C::NS ? u - (uint32_t)C::NS : u_first;
         for (uint32_t x = lo; x < u; ++x)
           drain_wait(&sh.full[x % C::NS], (x / C::NS) & 1);
-        if (off_last != 0xFFFFFFFFu) drain_wait(sh.off_full, off_last & 1);
         if (jbb_last != 0xFFFFFFFFu) {
           drain_wait(&sh.jbb_full[jbb_last & 1], (jbb_last >> 1) & 1);
           if (jbb_last > G0)
@@ -1887,13 +1798,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 
 // -------------------------------------------------------------- packing
 // B tiles: for block t, term, slice qq, tile j: rows r < width (column
-// qq*S + 256 j + r), k < 64 (spin 64 t + k), canonical no-swizzle K-major
+// qq*S + kTW j + r), k < 64 (spin 64 t + k), canonical no-swizzle K-major
 // order: ((r / 8) * 8 + k / 8) * 64 + (r % 8) * 8 + k % 8 (bf16 elements).
 __global__ void k_pack_tc_b(const float* Jt, int ld, int n, int F, int terms,
                             uint16_t* out) {
   const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
-  const int S = NP / F, NB = (n + 63) / 64, NT = (S + 255) / 256;
-  const int64_t tile = 256 * 64;
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + kTW - 1) / kTW;
+  const int64_t tile = (int64_t)kTW * 64;
   const int64_t total = (int64_t)NB * terms * F * NT * tile;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -1909,9 +1820,9 @@ __global__ void k_pack_tc_b(const float* Jt, int ld, int n, int F, int terms,
     const int cm = within / 64, inside = within % 64;
     const int r = (cm / 8) * 8 + inside / 8;
     const int k = (cm % 8) * 8 + inside % 8;
-    const int row = 64 * t + k, col = qq * S + 256 * j + r;
+    const int row = 64 * t + k, col = qq * S + kTW * j + r;
     float v = 0.0f;
-    if (row < n && col < n && r < 256 && 256 * j + r < S)
+    if (row < n && col < n && r < kTW && kTW * j + r < S)
       v = Jt[(int64_t)row * ld + col];
     const __nv_bfloat16 hi = __float2bfloat16_rn(v);
     const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
@@ -1953,8 +1864,8 @@ __global__ void k_repack_tc(const pysa_gb_problems p, int terms,
   const int64_t slot = sweep % (uint32_t)slots;
   const int F = n <= 512 ? 1 : (n <= 1024 ? 2 : 4);
   const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
-  const int S = NP / F, NB = (n + 63) / 64, NT = (S + 255) / 256;
-  const int64_t tile = 256 * 64;
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + kTW - 1) / kTW;
+  const int64_t tile = (int64_t)kTW * 64;
   const int64_t tb = (int64_t)NB * terms * F * NT * tile;
   const int64_t td = (int64_t)NB * 4096;
   uint16_t* bo = b_out + slot * b_stride + boff;
@@ -1974,9 +1885,9 @@ __global__ void k_repack_tc(const pysa_gb_problems p, int terms,
       const int cm = within / 64, inside = within % 64;
       const int r = (cm / 8) * 8 + inside / 8;
       const int k = (cm % 8) * 8 + inside % 8;
-      const int pos = 64 * t + k, col = qq * S + 256 * j + r;
+      const int pos = 64 * t + k, col = qq * S + kTW * j + r;
       float v = 0.0f;
-      if (pos < n && col < n && 256 * j + r < S)
+      if (pos < n && col < n && kTW * j + r < S)
         v = Jt[(int64_t)pi[pos] * ld + col];
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
       const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
@@ -2019,8 +1930,8 @@ int tc_fold_for(int n) {
 int64_t tc_b_elems(int n, int terms) {
   const int F = tc_fold_for(n);
   const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
-  const int S = NP / F, NB = (n + 63) / 64, NT = (S + 255) / 256;
-  return (int64_t)NB * terms * F * NT * 256 * 64;
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + kTW - 1) / kTW;
+  return (int64_t)NB * terms * F * NT * kTW * 64;
 }
 
 int64_t tc_diag_elems(int n) { return (int64_t)((n + 63) / 64) * 4096; }
