@@ -1667,8 +1667,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             for (int k = 0; k < F && ok; ++k)
               for (int jj = 0; jj < NT && ok; ++jj) {
                 const int j = jj == 0 ? jf : (jj <= jf ? jj - 1 : jj);
-                for (int term = 0; term < T && ok; ++term)
+                for (int term = 0; term < T && ok; ++term) {
                   ok = issue_stage(Bs, t, term, (qn + k) % F, j);
+                  if (k * NT + jj < 4 && term == 0) stamp(a, Gb, 16 + k * NT + jj);
+                }
               }
             stamp(a, Gb, 7);
           }
