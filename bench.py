@@ -965,6 +965,7 @@ def run_reference_arm(args, w, rank, world):
     J = P.copy()
     np.fill_diagonal(J, 0)
     R, n, Rd = w["replicas"], w["n"], w["reads"]
+    update = w.get("update", "sequential")
     betas = ladder(w)
 
     def chains(reads):
@@ -982,7 +983,7 @@ def run_reference_arm(args, w, rank, world):
     t0 = time.perf_counter()
     oracle.pt_run(ptype, J, h, betas, x, np.zeros((4, R), np.float32),
                   np.tile(np.arange(R, dtype=np.int32), (4, 1)), seed=1,
-                  num_sweeps=1, update=w["update"])
+                  num_sweeps=1, update=update)
     per_read = (time.perf_counter() - t0) / 4
     # all the workload's reads unless one sweep of them would take over
     # about 3 s (4 reads overestimate the per-read time: few chains per
@@ -999,7 +1000,7 @@ def run_reference_arm(args, w, rank, world):
         t0 = time.perf_counter()
         out = oracle.pt_run(ptype, J, h, betas, st["spins"], st["energies"],
                             st["beta_idx"], seed=1, num_sweeps=per_step,
-                            first_sweep=sweep, update=w["update"], best=best)
+                            first_sweep=sweep, update=update, best=best)
         dt = time.perf_counter() - t0
         sweep += per_step
         st = out
