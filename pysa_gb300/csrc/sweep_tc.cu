@@ -1319,10 +1319,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             fence_proxy_async();
           }
           }
-          if (lane == 0) {
-            stamp(a, Gb, 20 + warp);
-            stat_s[(Gb & 1) * 4 + warp] = blk_mf;
-          }
+          if (lane == 0) stat_s[(Gb & 1) * 4 + warp] = blk_mf;
           named_sync_128();
           {
             uint32_t mf = 0u;
@@ -1556,6 +1553,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 const bool crit = !RND && jj == 0 && k == 0 && has_next;
                 for (int term = 0; term < T; ++term) {
                   const uint32_t slot = (u + term) % C::NS;
+                  if (k * NT + jj < 4 && term == 0) stamp(a, Gb, 20 + k * NT + jj);
                   if (!tc_wait(&sh.full[slot], ((u + term) / C::NS) & 1, sh,
                                status)) {
                     ok = false;
