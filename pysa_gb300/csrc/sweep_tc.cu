@@ -231,6 +231,17 @@ __device__ __forceinline__ int cidx(int c, int k) {
   return c * 64 + ((((k >> 2) ^ (c & 7)) << 2) | (k & 3));
 }
 
+// The log-uniform buffers hold a = log u - m, m = 3e-5 + 1e-6 |log u|: the
+// rejection bound in the log domain, so that the rejection threshold in
+// field units is a / (beta scale) and the acceptance threshold
+// min((a + 2 m') / (beta scale), 0) with m' = 3e-5 + 1e-6 |a| >= m (a slightly
+// wider band: decisions outside it stay certain).  lf_of(a) = a + m' is a
+// log u estimate within 1e-9 relative, well inside the margin of
+// metropolis_accept_lf, for its exact rule.
+__device__ __forceinline__ float lf_of(float a) {
+  return a + fmaf(1e-6f, fabsf(a), 3e-5f);
+}
+
 __device__ __forceinline__ uint32_t bf16_bits(float d) {
   // exact for d in {0, +-1, +-2}
   return __float_as_uint(d) >> 16;
@@ -310,7 +321,7 @@ __device__ __noinline__ void redo_subblock(const RedoCtx& x, uint32_t* wcur,
     const float dn =
         x.ising ? (sbit ? 2.0f * hk : -2.0f * hk) : (sbit ? hk : -hk);
     const bool acc = x.valid && k < x.kmax &&
-                     metropolis_accept_lf(dn, x.beta, x.lfb[cidx(c, k)],
+                     metropolis_accept_lf(dn, x.beta, lf_of(x.lfb[cidx(c, k)]),
                                           x.seed, x.inst, x.sweep,
                                           x.chain_local, (uint32_t)(x.i0 + k));
     const float dl =
@@ -935,11 +946,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               float w[64];
 #pragma unroll
               for (int k = 0; k < 64; ++k) {
-                const float lfk = lfb[cidx(c, k)];
-                const float tl = lfk * invbs - fmaf(band1, fabsf(lfk), band0);
-                const uint32_t neg =
-                    ((k < 32 ? ~o0 >> k : ~o1 >> (k - 32)) & 1u) << 31;
-                w[k] = __uint_as_float((__float_as_uint(tl) & 0x7fffffffu) | neg);
+                const float tl = lfb[cidx(c, k)] * invbs;  // -|tl|
+                const bool sbit =
+                    ((k < 32 ? o0 >> k : o1 >> (k - 32)) & 1u) != 0u;
+                w[k] = sbit ? -tl : tl;
               }
               const uint64_t live64 =
                   kmax >= 64 ? ~0ull : ((1ull << kmax) - 1ull);
@@ -994,14 +1004,15 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   const bool sbit =
                       ((js < 32 ? o0 >> js : o1 >> (js - 32)) & 1u) != 0u;
                   const float x = sbit ? hj : -hj;
-                  const float lfk = lfb[cidx(c, js)];
+                  const float ak = lfb[cidx(c, js)];
                   const float th = fminf(
-                      fmaf(lfk, invbs, fmaf(band1, fabsf(lfk), band0)), 0.0f);
+                      fmaf(2.0f * band1, fabsf(ak), fmaf(ak, invbs, 2.0f * band0)),
+                      0.0f);
                   bool acc = x >= th;
                   if (!acc) {
                     // inside the band: the exact rule
                     acc = metropolis_accept_lf(
-                        scale * x, beta, lfk,
+                        scale * x, beta, lf_of(ak),
                         chain_seed(a.seed, a.s.stream_key, chain),
                         (uint32_t)inst, sweep, chain_local, (uint32_t)(i0 + js));
                   }
@@ -1085,11 +1096,10 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     #pragma unroll
               for (int j = 0; j < 16; ++j) {
                 const int k = 16 * g + j;
-                const float lfk = lfv[j];
-                const float t = lfk * invbs;
-                const float m = fmaf(band1, fabsf(lfk), band0);
-                const float th = fminf(t + m, 0.0f);
-                const float tl = t - m;
+                const float ak = lfv[j];
+                const float tl = ak * invbs;
+                const float th =
+                    fminf(fmaf(2.0f * band1, fabsf(ak), tl + 2.0f * band0), 0.0f);
                 const bool sbit = (sbits >> j) & 1u;
                 const float x = sbit ? hs[j] : -hs[j];
                 // positions past n have zero fields (x = 0 >= th): their
@@ -1697,9 +1707,20 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               uint32_t x[4];
               draw4(sk, TAG_SWEEP, (uint32_t)inst, sweep, cl,
                     (uint32_t)(16 * t + quad), x);
-              *reinterpret_cast<float4*>(out + cidx(c2, 4 * quad)) =
-                  make_float4(log_uniform_f32(x[0]), log_uniform_f32(x[1]),
-                              log_uniform_f32(x[2]), log_uniform_f32(x[3]));
+              // a = log u - m: the rejection bound in the log domain, m =
+              // 3e-5 + 1e-6 |log u| the band of the f32 log (over three
+              // times the error of __logf plus the roundings of a
+              // threshold); the deciders scale it by 1 / (beta scale)
+              float4 v;
+              v.x = log_uniform_f32(x[0]);
+              v.y = log_uniform_f32(x[1]);
+              v.z = log_uniform_f32(x[2]);
+              v.w = log_uniform_f32(x[3]);
+              v.x -= fmaf(1e-6f, fabsf(v.x), 3e-5f);
+              v.y -= fmaf(1e-6f, fabsf(v.y), 3e-5f);
+              v.z -= fmaf(1e-6f, fabsf(v.z), 3e-5f);
+              v.w -= fmaf(1e-6f, fabsf(v.w), 3e-5f);
+              *reinterpret_cast<float4*>(out + cidx(c2, 4 * quad)) = v;
             }
           }
           if constexpr (RND) {
