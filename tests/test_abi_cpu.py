@@ -85,6 +85,18 @@ def test_null_arguments_rejected_without_gpu():
     assert lib.pysa_gb_logz_parts(1, 40) == -1
 
 
+def test_decision_mode_setter_validates_without_gpu():
+    """pysa_gb_set_decision_mode takes 0 (per block), 1 (block rounds) or 2
+    (sequential sub-blocks) and rejects anything else with an error."""
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    for bad in (-1, 3, 7):
+        assert lib.pysa_gb_set_decision_mode(bad) == -1
+        assert b"decision mode" in lib.pysa_gb_last_error()
+    for good in (1, 2, 0):
+        assert lib.pysa_gb_set_decision_mode(good) == 0
+
+
 def test_pack_unpack_roundtrip():
     from pysa_gb300.engine import pack_spins, unpack_spins
     rng = np.random.default_rng(0)
