@@ -212,6 +212,12 @@ typedef struct {
    * by pysa_gb_tc_setup; pysa_gb_tc_workspace sizes for the smallest
    * items any value can give. */
   int32_t tc_item_chains;
+  /* host, from pysa_gb_tc_setup: bit v set when every work item of fold
+   * variant v (F = 1, 2, 4) belongs to an instance of the same n.  Fused
+   * launches of such a variant, with tc_unit_sweeps = 0, split the launch's
+   * item-sweeps evenly over the CTAs (wrap-around units) instead of running
+   * fixed-length units from a queue. */
+  int32_t tc_uniform;
 } pysa_gb_workspace;
 
 /* Host copies of the per-instance tables, used to plan the work list. */
@@ -279,6 +285,19 @@ int pysa_gb_set_unit_wait_limit(uint64_t ns);
  * tests pin both forms.  Applies to launches enqueued after the call,
  * process-wide.  No counterpart in the reference. */
 int pysa_gb_set_decision_mode(int32_t mode);
+
+/* Decision mode 0's switch point: a block is decided in rounds while the
+ * previous block's largest flip count of a chain was at most `flips`
+ * (0..64, default 12), in sequential sub-blocks otherwise.  Same decisions
+ * for every value; process-wide, for launches enqueued after the call.  No
+ * counterpart in the reference. */
+int pysa_gb_set_block_round_limit(int32_t flips);
+
+/* Most CTAs of a tensor-core sweep launch (0, the default: one per SM).
+ * Results do not depend on it; a smaller value leaves SMs to other work and
+ * lets tests split few work items over fewer CTAs.  Process-wide, for
+ * launches enqueued after the call.  No counterpart in the reference. */
+int pysa_gb_set_tc_max_ctas(int32_t ctas);
 
 /* Workspace sizing and set-up.
  *   pysa_gb_workspace_bytes: sizes of the workspace arrays for a batch

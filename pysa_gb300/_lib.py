@@ -54,7 +54,8 @@ class Workspace(ctypes.Structure):
                 ("tc_rand_slots", I32), ("csr_item_start", I32),
                 ("csr_item_count", I32), ("csr_width", I32),
                 ("csr_chains", I32), ("wide_item_start", I32),
-                ("wide_item_count", I32), ("tc_item_chains", I32)]
+                ("wide_item_count", I32), ("tc_item_chains", I32),
+                ("tc_uniform", I32)]
 
 
 class HostTables(ctypes.Structure):
@@ -110,6 +111,8 @@ def load() -> ctypes.CDLL:
         "pysa_gb_set_trace": ([P], ctypes.c_int),
         "pysa_gb_set_unit_wait_limit": ([U64], ctypes.c_int),
         "pysa_gb_set_decision_mode": ([ctypes.c_int32], ctypes.c_int),
+        "pysa_gb_set_block_round_limit": ([ctypes.c_int32], ctypes.c_int),
+        "pysa_gb_set_tc_max_ctas": ([ctypes.c_int32], ctypes.c_int),
         "pysa_gb_last_error": ([], ctypes.c_char_p),
         "pysa_gb_workspace_bytes": ([I32, P, P], ctypes.c_int),
         "pysa_gb_setup": ([P, P, P, P], ctypes.c_int),

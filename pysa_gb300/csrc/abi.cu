@@ -53,6 +53,8 @@ static thread_local std::string g_last_error;
 static unsigned long long* g_tc_trace = nullptr;  // diagnostics, see below
 static uint64_t g_unit_wait_ns = 0;  // diagnostics: 0 = the default bound
 static int32_t g_decision_mode = 0;   // tensor-core sweep: 0 auto, 1, 2
+static int32_t g_round_limit = 12;    // mode 0: block rounds up to this
+static int32_t g_tc_max_ctas = 0;     // tensor-core launches: 0 = SM count
 
 static int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -141,6 +143,19 @@ int pysa_gb_set_decision_mode(int32_t mode) {
   if (mode < 0 || mode > 2)
     return fail(PYSA_GB_ERR_ARG, "decision mode must be 0, 1 or 2");
   g_decision_mode = mode;
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_set_block_round_limit(int32_t flips) {
+  if (flips < 0 || flips > 64)
+    return fail(PYSA_GB_ERR_ARG, "block round limit must be in 0..64");
+  g_round_limit = flips;
+  return PYSA_GB_OK;
+}
+
+int pysa_gb_set_tc_max_ctas(int32_t ctas) {
+  if (ctas < 0) return fail(PYSA_GB_ERR_ARG, "max CTAs must be >= 0");
+  g_tc_max_ctas = ctas;
   return PYSA_GB_OK;
 }
 
@@ -462,6 +477,7 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   const std::vector<int> isz =
       tc_item_sizes(p->num_instances, host, min_n, ws->tc_item_chains);
   const int folds[3] = {1, 2, 4};
+  int uniform = 0;
   for (int v = 0; v < 3; ++v) {
     ws->tc_variant_start[v] = (int32_t)items.size();
     for (int i = 0; i < p->num_instances; ++i) {
@@ -480,6 +496,11 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
       }
     }
     ws->tc_variant_count[v] = (int32_t)items.size() - ws->tc_variant_start[v];
+    bool same = true;
+    for (int k = ws->tc_variant_start[v] + 1; k < (int)items.size(); ++k)
+      same = same && host->n[items[k].inst] ==
+                         host->n[items[ws->tc_variant_start[v]].inst];
+    if (same) uniform |= 1 << v;
   }
   if (!items.empty()) {
     cudaError_t e = cudaMemcpyAsync(ws->tc_items, items.data(),
@@ -515,6 +536,7 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   // host vectors above are pageable: the copies are complete on return
   ws->plain_live = live;
   ws->tc_fusable = fusable;
+  ws->tc_uniform = uniform;
   ws->tc_enabled = 1;
   return PYSA_GB_OK;
 }
@@ -641,6 +663,9 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.exchange_every = o->exchange_every;
   ta.unit_wait_ns = g_unit_wait_ns;
   ta.decision_mode = g_decision_mode;
+  ta.round_limit = g_round_limit;
+  ta.wrap = 0;
+  ta.pad_wrap_ = 0;
   ta.sched = ws->tc_sched;
   ta.perm = ws->perm;
   ta.perm_slots = a.perm_slots;
@@ -650,13 +675,22 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.rand_b_stride = ws->tc_b_elems;
   ta.rand_diag_stride = ws->tc_diag_elems;
   ta.trace = g_tc_trace;
-  const int sms = sm_count();
+  const int sms = g_tc_max_ctas > 0 && g_tc_max_ctas < sm_count()
+                      ? g_tc_max_ctas
+                      : sm_count();
   const int folds[3] = {1, 2, 4};
   int last_v = -1;
   for (int v = 0; v < 3; ++v)
     if (ws->tc_variant_count[v] > 0) last_v = v;
+  // Fused launches over items of one size split the launch's item-sweeps
+  // evenly over the CTAs (wrap-around units) unless the caller fixed the
+  // unit length.
+  auto wraps = [&](int v, int fuse) {
+    return fuse && ws->tc_unit_sweeps == 0 && ((ws->tc_uniform >> v) & 1);
+  };
   // one persistent tensor-core launch per fold: `units` work units of
-  // `ku` sweeps per item, exchange fused or not
+  // `ku` sweeps per item (or wrap-around units over ku * units sweeps),
+  // exchange fused or not
   auto tc_launches = [&](int ku, int units, int fuse) -> int {
     for (int v = 0; v < 3; ++v) {
       const int count = ws->tc_variant_count[v];
@@ -667,8 +701,9 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
       ta.items = reinterpret_cast<const TcItem*>(ws->tc_items) +
                  ws->tc_variant_start[v];
       ta.num_items = count;
-      ta.unit_sweeps = ku;
-      ta.units_per_item = units;
+      ta.wrap = wraps(v, fuse) ? 1 : 0;
+      ta.unit_sweeps = ta.wrap ? ku * units : ku;
+      ta.units_per_item = ta.wrap ? 1 : units;
       ta.fuse_exchange = fuse;
       ta.advance_counter = fuse && v == last_v;
       e = launch_tc(ta, folds[v], random, sms, st);
@@ -701,14 +736,18 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
       per_launch = ws->tc_rand_slots;
     // items of the largest fold: its launch sets the number of unit waves
     int items = 1;
-    for (int v = 0; v < 3; ++v)
+    bool all_wrap = true;
+    for (int v = 0; v < 3; ++v) {
       if (ws->tc_variant_count[v] > items) items = ws->tc_variant_count[v];
+      if (ws->tc_variant_count[v] > 0 && !wraps(v, 1)) all_wrap = false;
+    }
     int remaining = num_sweeps;
     while (remaining > 0) {
       int chunk = remaining < per_launch ? remaining : per_launch;
       const int ku = ws->tc_unit_sweeps > 0
                          ? (chunk < ku_pref ? chunk : ku_pref)
-                         : tc_unit_for(chunk, ku_pref, items, sms);
+                     : all_wrap ? chunk
+                                : tc_unit_for(chunk, ku_pref, items, sms);
       chunk = chunk / ku * ku;
       if (random) {
         const int rc = rand_prepare(chunk);

@@ -39,10 +39,9 @@ namespace pysa_gb {
 constexpr int kTW = 256;
 
 // Decision mode of a block: block rounds (D64) while the previous block's
-// largest flip count of any chain was at most this, else sequential
-// sub-blocks.  A round costs about as much as 6-10 sequential spins, so the
-// rounds win while flips are rare.
-constexpr uint32_t kD64MaxFlips = 12;
+// largest flip count of any chain was at most TcArgs::round_limit (default
+// 12), else sequential sub-blocks.  A round costs about as much as 6-10
+// sequential spins, so the rounds win while flips are rare.
 
 // RND: random visiting order (one permutation per instance and sweep); the
 // B ring keeps two stages to make room for the gathered block fields.
@@ -103,9 +102,10 @@ struct TcCfg {
   // lf_full[2], lf_free[2], full[NS], free[NS], drain, mma_done_b[2]
   static constexpr int NBARS = 16 + 2 * NS;
   static constexpr size_t MISC_OFF = BAR_OFF + NBARS * 8;
-  // tmem slot, abort flag, current unit, then per block parity and decision
-  // warp the block's largest flip count of a chain ([2][4] int32)
-  static constexpr size_t STAT_OFF = MISC_OFF + 24;
+  // tmem slot, abort flag, current unit (item, first sweep, sweeps), then
+  // per block parity and decision warp the block's largest flip count of a
+  // chain ([2][4] int32)
+  static constexpr size_t STAT_OFF = MISC_OFF + 32;
   static constexpr size_t BYTES = STAT_OFF + 32;
   static_assert(BYTES <= 232448, "shared memory budget");
 };
@@ -348,12 +348,55 @@ __device__ __noinline__ void redo_subblock(const RedoCtx& x, uint32_t* wcur,
   *dEb = e;
 }
 
-// Work units: unit u is item u % num_items for sweeps
-// sweep0 + (u / num_items) * unit_sweeps ... + unit_sweeps - 1.  CTAs take
-// units from a queue in order; a unit waits (bounded) until the same item's
-// previous unit is done, which a CTA that is already running owns, so the
-// wait always ends.  Within a unit the fields stay in TMEM across sweeps; the
-// replica exchange of the item's reads runs in the kernel when fused.
+// Wrap-around split of a launch's num_items * S item-sweeps over m CTAs
+// (McNaughton's rule for preemptive scheduling on identical machines): share
+// k holds positions [k T / m, (k + 1) T / m) of the item-major order (sweep s
+// of item i at i S + s, T = num_items S), and num_items >= m makes every
+// share at least S long.  Its pieces, in order: the head of the item the
+// share ends in (sweeps 0 .. p1 % S - 1), its whole items, then the tail of
+// the item it starts in (sweeps p0 % S .. S - 1).  That tail's head is the
+// first piece of share k - 1 and, with sweeps of equal cost, is done before
+// the tail starts.  Piece j of share k -> (item, first sweep, sweeps);
+// false past the last piece.
+__device__ __forceinline__ bool wrap_piece(int items, int S, int m, int k,
+                                           int j, int* it, int* sb, int* sl) {
+  const int64_t T = (int64_t)items * S;
+  const int64_t p0 = T * k / m, p1 = T * (k + 1) / m;
+  const int head = (int)(p1 % S), tail = (int)(p0 % S);
+  const int64_t f0 = (p0 + S - 1) / S, f1 = p1 / S;  // whole items [f0, f1)
+  if (head) {
+    if (j == 0) {
+      *it = (int)(p1 / S);
+      *sb = 0;
+      *sl = head;
+      return true;
+    }
+    --j;
+  }
+  if (j < f1 - f0) {
+    *it = (int)(f0 + j);
+    *sb = 0;
+    *sl = S;
+    return true;
+  }
+  if (tail && j == f1 - f0) {
+    *it = (int)(p0 / S);
+    *sb = tail;
+    *sl = S - tail;
+    return true;
+  }
+  return false;
+}
+
+// Work units.  Fixed units (a.wrap == 0): unit u is item u % num_items for
+// sweeps (u / num_items) * unit_sweeps ... + unit_sweeps - 1 of the launch,
+// taken from a queue in order.  Wrap-around units (a.wrap == 1, items of one
+// size, unit_sweeps = the launch's sweeps): each CTA takes a share from the
+// queue and runs its pieces (wrap_piece).  Either way a unit waits (bounded)
+// until its item has run the sweeps before it, which a CTA that took its
+// work from the queue earlier (so is running) owns, so the wait always ends.
+// Within a unit the fields stay in TMEM across sweeps; the replica exchange
+// of the item's reads runs in the kernel when fused.
 template <int F, bool RND>
 __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   using C = TcCfg<F, RND>;
@@ -377,7 +420,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                                           // buffer 0 / 1 (two buffers)
   sh.tmem_slot = reinterpret_cast<uint32_t*>(smem + C::MISC_OFF);
   sh.abort = reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 8);
-  volatile int32_t* unit_s =
+  volatile int32_t* unit_s =  // [item, first sweep, sweeps] of the unit
       reinterpret_cast<volatile int32_t*>(smem + C::MISC_OFF + 16);
   volatile uint32_t* stat_s =
       reinterpret_cast<volatile uint32_t*>(smem + C::STAT_OFF);
@@ -411,7 +454,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   int32_t* status = a.s.status;
   const bool ising = a.p.problem_type == PYSA_GB_ISING;
   const uint32_t sweep0 = (uint32_t)(*a.s.sweep_counter);
-  const int KU = a.unit_sweeps;
   const int total_units = a.num_items * a.units_per_item;
   const int T = a.terms;
   constexpr uint32_t kCols = 512;
@@ -450,27 +492,39 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   // decision warps: this block's decision mode (the same in all 128 threads);
   // sequential until a block shows few flips
   bool d64 = a.decision_mode == 1;
+  int share = -1, piece = 0;  // thread 0, wrap-around units
 
   for (;;) {
     // ------------------------------------------------------ next unit
     if (threadIdx.x == 0) {
-      int un = -1;
+      int it = -1, sb = 0, sl = 0;
       if (!*sh.abort) {
-        un = (int)atomicAdd(reinterpret_cast<unsigned*>(a.sched), 1u);
-        if (un >= total_units) {
-          un = -1;
+        if (a.wrap) {
+          if (share < 0)
+            share = (int)atomicAdd(reinterpret_cast<unsigned*>(a.sched), 1u);
+          if (!wrap_piece(a.num_items, a.unit_sweeps, (int)gridDim.x, share,
+                          piece++, &it, &sb, &sl))
+            it = -1;
         } else {
-          const int it = un % a.num_items, ch = un / a.num_items;
-          volatile int32_t* done = a.sched + 2 + it;
-          if (*done < ch) {
+          const int un =
+              (int)atomicAdd(reinterpret_cast<unsigned*>(a.sched), 1u);
+          if (un < total_units) {
+            it = un % a.num_items;
+            sb = (un / a.num_items) * a.unit_sweeps;
+            sl = a.unit_sweeps;
+          }
+        }
+        if (it >= 0) {
+          volatile int32_t* done = a.sched + 2 + it;  // sweeps run
+          if (*done < sb) {
             const uint64_t lim =
                 a.unit_wait_ns ? a.unit_wait_ns : 1000000000ull;
             const uint64_t t0 = globaltimer_ns();
-            while (*done < ch) {
+            while (*done < sb) {
               if (globaltimer_ns() - t0 > lim) {
                 set_status(status, PYSA_GB_ERR_TIMEOUT);
                 *sh.abort = 1;
-                un = -1;
+                it = -1;
                 break;
               }
             }
@@ -478,14 +532,17 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           __threadfence();  // the previous unit's stores are visible
         }
       }
-      *unit_s = un;
+      unit_s[0] = it;
+      unit_s[1] = sb;
+      unit_s[2] = sl;
     }
     __syncthreads();
-    const int un = *unit_s;
-    if (un < 0) break;
-    const TcItem item = a.items[un % a.num_items];
-    const int chunk = un / a.num_items;
-    const uint32_t sweep_first = sweep0 + (uint32_t)(chunk * KU);
+    const int un_item = unit_s[0];
+    if (un_item < 0) break;
+    const int un_first = unit_s[1];
+    const int KU = unit_s[2];
+    const TcItem item = a.items[un_item];
+    const uint32_t sweep_first = sweep0 + (uint32_t)un_first;
     const int inst = item.inst;
     const int n = a.p.n[inst];
     const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
@@ -1336,7 +1393,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
             for (int w4 = 0; w4 < 4; ++w4) mf = max(mf, stat_s[(Gb & 1) * 4 + w4]);
             d64 = a.decision_mode == 1 ||
-                  (a.decision_mode == 0 && mf <= kD64MaxFlips);
+                  (a.decision_mode == 0 && (int)mf <= a.round_limit);
           }
           if (threadIdx.x == 0) {
             stamp(a, Gb, 4);
@@ -1796,8 +1853,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
     if (threadIdx.x == 0) {
       stamp_cta(a, 4);
       __threadfence();  // this unit's stores before its done flag
-      atomicExch(reinterpret_cast<int*>(a.sched + 2 + un % a.num_items),
-                 chunk + 1);
+      atomicExch(reinterpret_cast<int*>(a.sched + 2 + un_item),
+                 un_first + KU);
     }
   }
 

@@ -26,18 +26,21 @@ struct TcArgs {
   uint64_t seed;
   int32_t recompute_every;  // >0: H and E rebuilt when sweep % this == 0
   int32_t num_items;        // items of this fold
-  int32_t unit_sweeps;      // sweeps per work unit
-  int32_t units_per_item;   // work units per item in this launch
+  int32_t unit_sweeps;      // sweeps per work unit (wrap: of the launch)
+  int32_t units_per_item;   // work units per item in this launch (wrap: 1)
+  int32_t wrap;             // 1: wrap-around units (items of one size)
+  int32_t pad_wrap_;
   int32_t fuse_exchange;    // 1: exchange inside the kernel (R | chains/CTA)
   int32_t use_pt;
   int32_t advance_counter;  // 1: the last CTA advances the sweep counter
   int32_t exchange_every;   // <= 1: every sweep; k: after (s + 1) % k == 0
   uint64_t unit_wait_ns;  // bound of the wait for an item's previous unit
-  int32_t decision_mode;  // 0 per-block choice, 1 block rounds, 2 sub-blocks
-  int32_t pad_mode_;
                           // (0: one second)
+  int32_t decision_mode;  // 0 per-block choice, 1 block rounds, 2 sub-blocks
+  int32_t round_limit;    // mode 0: block rounds while the previous block's
+                          // largest flip count of a chain is at most this
   int32_t* sched;  // zeroed per launch: [0] unit queue, [1] finished CTAs,
-                   // [2 + item] units of the item done
+                   // [2 + item] sweeps of the item run in this launch
   // random order: permutation of (inst, sweep) at
   // perm[((sweep % perm_slots) * num_instances + inst) * max_n]; tiles and
   // diagonal blocks repacked in that order at slot sweep % rand_slots
@@ -59,7 +62,8 @@ int64_t tc_diag_elems(int n);
 cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
                            uint16_t* b_out, float* diag_out, cudaStream_t st);
 // Persistent launch over a.num_items * a.units_per_item work units with at
-// most `max_ctas` CTAs; a.sched must hold 2 + num_items zeroed words.
+// most `max_ctas` CTAs (wrap: min(num_items, max_ctas) CTAs, one share of
+// the item-sweeps each); a.sched must hold 2 + num_items zeroed words.
 // random: visiting order from a.perm, tiles from a.rand_b / a.rand_diag.
 cudaError_t launch_tc(const TcArgs& a, int F, bool random, int max_ctas,
                       cudaStream_t st);

@@ -97,6 +97,22 @@ def test_decision_mode_setter_validates_without_gpu():
         assert lib.pysa_gb_set_decision_mode(good) == 0
 
 
+def test_schedule_knobs_validate_without_gpu():
+    """pysa_gb_set_block_round_limit takes 0..64 and pysa_gb_set_tc_max_ctas
+    any count >= 0 (0: one CTA per SM); both reject the rest."""
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    for bad in (-1, 65):
+        assert lib.pysa_gb_set_block_round_limit(bad) == -1
+        assert b"round limit" in lib.pysa_gb_last_error()
+    assert lib.pysa_gb_set_tc_max_ctas(-2) == -1
+    assert b"max CTAs" in lib.pysa_gb_last_error()
+    for good in (0, 64, 12):
+        assert lib.pysa_gb_set_block_round_limit(good) == 0
+    assert lib.pysa_gb_set_tc_max_ctas(5) == 0
+    assert lib.pysa_gb_set_tc_max_ctas(0) == 0
+
+
 def test_pack_unpack_roundtrip():
     from pysa_gb300.engine import pack_spins, unpack_spins
     rng = np.random.default_rng(0)

@@ -5,18 +5,41 @@ The dense-QUBO workload (n = 1024, Q_ij integers in [-8, 8], diagonal in
 [-16, 16], 64 replicas on a geometric 0.5-8.0 temperature ladder) runs on the
 persistent tensor-core sweep at fold 2 (64 chains per CTA).  R = 64 divides
 the chains per CTA, so the replica exchange runs inside the kernel and one
-launch covers up to 128 sweeps in work units of 8.  These tests drive that
-path -- fused exchange, unit boundaries, launch boundaries, the short tail
-units of a run whose length is not a multiple of 8, and CUDA-graph replays --
-and compare every returned array with the oracle (pysa/simulation.py:150-171,
-pysa/qubo.py:40-63, pysa/utils.py:44-58 on the shared Philox stream).
-Integer couplings make every product and sum exact, so equality is required.
-The same at fold 4 (n = 1300, 32 chains per CTA, R = 32).
+launch covers up to 128 sweeps.  Work items of one instance size split a
+launch's item-sweeps evenly over the CTAs (wrap-around units: a CTA runs the
+first sweeps of one item, whole items, then the last sweeps of an item whose
+first sweeps another CTA ran); with the unit length fixed by the caller,
+CTAs take fixed-length units from a queue instead.  These tests drive that
+path under three schedules -- one CTA per item, wrap-around units split over
+two CTAs, fixed 8-sweep units -- with fused exchange, unit and launch
+boundaries, runs whose length is not a multiple of 8, and CUDA-graph
+replays, and compare every returned array with the oracle
+(pysa/simulation.py:150-171, pysa/qubo.py:40-63, pysa/utils.py:44-58 on the
+shared Philox stream).  Integer couplings make every product and sum exact,
+so equality is required.  The same at fold 4 (n = 1300, 32 chains per CTA,
+R = 32) and fold 1.
 """
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+SCHEDULES = ["per_item", "wrap2", "fixed8"]
+
+
+@pytest.fixture
+def schedule_knobs():
+    """Applies a schedule to a batch; puts the process-wide CTA cap back."""
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+
+    def apply(b, schedule):
+        if schedule == "fixed8":
+            b.ws.tc_unit_sweeps = 8
+        _lib.check(lib.pysa_gb_set_tc_max_ctas(
+            2 if schedule == "wrap2" else 0), "max ctas")
+    yield apply
+    _lib.check(lib.pysa_gb_set_tc_max_ctas(0), "max ctas reset")
 
 
 def _qubo(rng, n):
@@ -58,7 +81,7 @@ def _fused_batch(ptype, J, h, betas, Rd, fold):
 
 
 def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
-                   fold, graph_chunk=128):
+                   fold, graph_chunk=128, knobs=None, schedule="per_item"):
     """plan: the sweep counts of consecutive run() calls on one batch (each
     call continues the previous one's chains, as Solver resumes)."""
     from pysa_gb300 import pack_spins
@@ -72,6 +95,10 @@ def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
     e0 = np.array([[oracle.energy64(J, h, s) for s in r] for r in x0],
                   np.float32)
     b = _fused_batch(ptype, J, h, betas, Rd, fold)
+    if knobs is not None:
+        knobs(b, schedule)
+    if schedule != "fixed8":
+        assert b.ws.tc_uniform & (1 << {1: 0, 2: 1, 4: 2}[fold])
     b.set_states(pack_spins(x0, ptype, b.words), e0)
     bidx = np.tile(np.arange(R, dtype=np.int32), (Rd, 1))
     state = (x0, e0, bidx, None)
@@ -90,20 +117,25 @@ def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
     assert int(b.sweep_counter.item()) == done
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("plan", [(136,), (20,), (20, 13, 1)])
-def test_headline_qubo1024_fold2_fused_bit_exact(oracle, plan):
-    """136 sweeps: a 128-sweep launch of sixteen 8-sweep units, then one
-    8-sweep launch.  20 and 20 + 13 + 1: runs whose length is not a multiple
-    of the unit, resumed across calls."""
+def test_headline_qubo1024_fold2_fused_bit_exact(oracle, schedule_knobs,
+                                                 plan, schedule):
+    """136 sweeps: a 128-sweep launch, then an 8-sweep one (fixed8: sixteen
+    8-sweep units, then one; wrap2: three items over two CTAs, the middle
+    item split at sweep 64, then at sweep 4).  20 and 20 + 13 + 1: runs
+    whose length is not a multiple of 8, resumed across calls."""
     _run_vs_oracle(oracle, "qubo", 1024, 64, 3, 0.5, 8.0, plan, seed=11,
-                   fold=2)
+                   fold=2, knobs=schedule_knobs, schedule=schedule)
 
 
-def test_headline_qubo1024_fold2_graph_replay_bit_exact(oracle):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_headline_qubo1024_fold2_graph_replay_bit_exact(oracle, schedule_knobs,
+                                                        schedule):
     """300 sweeps as run() issues them for long runs: two replays of a
     captured 128-sweep graph, then 44 sweeps issued directly."""
-    _run_vs_oracle(oracle, "qubo", 1024, 64, 2, 0.5, 8.0, (300,), seed=12,
-                   fold=2)
+    _run_vs_oracle(oracle, "qubo", 1024, 64, 3, 0.5, 8.0, (300,), seed=12,
+                   fold=2, knobs=schedule_knobs, schedule=schedule)
 
 
 def test_headline_ising_pm1_fold2_fused_bit_exact(oracle):
@@ -111,12 +143,26 @@ def test_headline_ising_pm1_fold2_fused_bit_exact(oracle):
                    fold=2)
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("plan", [(136,), (20,)])
-def test_fold4_qubo1300_fused_bit_exact(oracle, plan):
+def test_fold4_qubo1300_fused_bit_exact(oracle, schedule_knobs, plan,
+                                        schedule):
     _run_vs_oracle(oracle, "qubo", 1300, 32, 3, 0.5, 8.0, plan, seed=14,
-                   fold=4)
+                   fold=4, knobs=schedule_knobs, schedule=schedule)
 
 
-def test_fold1_qubo512_fused_bit_exact(oracle):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_fold1_qubo512_fused_bit_exact(oracle, schedule_knobs, schedule):
     _run_vs_oracle(oracle, "qubo", 512, 32, 4, 0.5, 8.0, (136,), seed=15,
-                   fold=1)
+                   fold=1, knobs=schedule_knobs, schedule=schedule)
+
+
+def test_wrap_split_many_items_bit_exact(oracle, schedule_knobs):
+    """Seven items over three CTAs, run lengths 128 and 9: the first CTA
+    runs the head of item 2 and items 0-1, the second the head of item 4,
+    item 3 and the tail of item 2, the third items 5-6 and the tail of
+    item 4."""
+    from pysa_gb300 import _lib
+    _lib.check(_lib.load().pysa_gb_set_tc_max_ctas(3), "max ctas")
+    _run_vs_oracle(oracle, "qubo", 1024, 64, 7, 0.5, 8.0, (137,), seed=16,
+                   fold=2)

@@ -6,9 +6,10 @@ frees its tensor memory and returns, and the host raises.  This test makes a
 wait run out on purpose without faulting anything: the wait for a work
 item's previous unit happens at a unit's start, when the CTA has nothing in
 flight, and pysa_gb_set_unit_wait_limit shrinks its bound to a few
-microseconds.  One work item run for 128 sweeps in one launch is split into
-several units taken by as many CTAs at once, so the CTAs holding units 1 and
-later must wait for unit 0 (hundreds of microseconds) and give up.  The
+microseconds.  One work item run for 128 sweeps in one launch with the unit
+length fixed at 8 sweeps is split into sixteen units taken by as many CTAs
+at once, so the CTAs holding units 1 and later must wait for unit 0
+(hundreds of microseconds) and give up.  The
 batch and the context must stay usable: the next run, with the default
 bound, matches the oracle bit for bit.
 """
@@ -30,6 +31,7 @@ def test_unit_wait_timeout_reported_and_batch_reusable(oracle):
     b = PTBatch("qubo", [Instance(Q, h, betas, Rd)], kernel="tc")
     assert b.ws.tc_fusable == 1 and b.ws.plain_live == 0
     lib = _lib.load()
+    b.ws.tc_unit_sweeps = 8                     # fixed units from the queue
     b.set_states(pack_spins(x0, "qubo", b.words), None)
     try:
         lib.pysa_gb_set_unit_wait_limit(2000)   # 2 us
