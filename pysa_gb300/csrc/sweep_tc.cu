@@ -83,6 +83,9 @@ struct TcCfg {
   static constexpr bool HELP = F == 2;
   // F == 4: the three idle slices' warps write the A rows of sub-blocks 0-2
   static constexpr bool APUT = F == 4;
+  // F == 2, visiting order: block rounds run on all four decision warps,
+  // two lanes per chain (the other slice's warps would idle)
+  static constexpr bool PAIRS = F == 2 && !RND;
   static constexpr size_t CORR_OFF = BETA_OFF + CC * 4;
   static constexpr size_t CORR_BYTES = HELP ? (size_t)2 * 16 * CC * 4 : 0;
   // RND, F > 1: fields of the block's 64 scattered columns, gathered by the
@@ -805,7 +808,197 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             named_sync_128();
           }
           uint32_t blk_mf = 0u;  // largest flip count of a chain (deciders)
-          {
+          if (C::PAIRS && d64) {
+            // ------------------- block rounds on the four decision warps
+            // The slice holding the block loads its 64 fields from TMEM into
+            // dl_s ([chain][64], swizzled); then every chain is decided by
+            // two lanes of one warp: lane (cc, hf), cc = 16 warp + lane % 16,
+            // hf = lane / 16, tests positions 32 hf .. 32 hf + 31, its
+            // partner is lane ^ 16.  Each round both lanes take the chain's
+            // first candidate over all 64 positions (the partner's mask by
+            // shuffle) and decide it identically; an accepted flip corrects
+            // each lane's half of the fields.  The decisions, and every
+            // rounding on their way, are those of the one-lane rounds below.
+            const int hf = lane >> 4, cc = 16 * warp + (lane & 15);
+            bool ok = !*sh.abort;
+            if (ok && q == qt && wait_h)
+              ok = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
+            if (ok) ok = tc_wait(&sh.jbb_full[Gb & 1], (Gb >> 1) & 1, sh, status);
+            if (ok) ok = tc_wait(&sh.lf_full[Gb & 1], (Gb >> 1) & 1, sh, status);
+            ok = __all_sync(0xffffffffu, ok);
+            if (L == 0) stamp(a, Gb, 0);
+            if (L == 0) stamp(a, Gb, 1);
+            if (ok && q == qt) {
+              tc::fence_after_sync();
+              float hl[64];
+              tc::tmem_ld64(taddr + lane_base + co, hl);
+#pragma unroll
+              for (int q4 = 0; q4 < 16; ++q4)
+                *reinterpret_cast<float4*>(dl_s + cidx(c, 4 * q4)) =
+                    make_float4(hl[4 * q4], hl[4 * q4 + 1], hl[4 * q4 + 2],
+                                hl[4 * q4 + 3]);
+            }
+            named_sync_128();  // the fields are in dl_s
+            if (L == 0) stamp(a, Gb, 8);
+            ok = __all_sync(0xffffffffu, ok && !*sh.abort);
+            if (ok) {
+              const bool pvalid = cc < item.nchains;
+              const float* jb = jbb + (Gb & 1) * 4096;
+              const float* lfb = lf_s + (Gb & 1) * 64 * CC;
+              const uint32_t o0 = spins_s[(2 * t) * CC + cc];
+              const uint32_t o1 = spins_s[(2 * t + 1) * CC + cc];
+              const uint32_t om = hf ? o1 : o0;  // this lane's half
+              const float pbeta = beta_s[cc];
+              const float scale = ising ? 2.0f : 1.0f;
+              const float invbs =
+                  pbeta > 0.0f ? 1.0f / (pbeta * scale) : INFINITY;
+              const bool banded = pvalid && invbs < INFINITY;
+              const float band0 = banded ? 3e-5f * invbs : 0.0f;
+              const float band1 = banded ? 1e-6f * invbs : 0.0f;
+              float h[32], w[32];
+#pragma unroll
+              for (int q4 = 0; q4 < 8; ++q4) {
+                const float4 v = *reinterpret_cast<const float4*>(
+                    dl_s + cidx(cc, 32 * hf + 4 * q4));
+                h[4 * q4 + 0] = v.x;
+                h[4 * q4 + 1] = v.y;
+                h[4 * q4 + 2] = v.z;
+                h[4 * q4 + 3] = v.w;
+              }
+#pragma unroll
+              for (int q4 = 0; q4 < 8; ++q4) {
+                const float4 v = *reinterpret_cast<const float4*>(
+                    lfb + cidx(cc, 32 * hf + 4 * q4));
+                const float av[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                  const int k = 4 * q4 + i;
+                  const float tl = av[i] * invbs;  // -|tl|
+                  w[k] = ((om >> k) & 1u) ? -tl : tl;
+                }
+              }
+              const uint64_t live64 =
+                  kmax >= 64 ? ~0ull : ((1ull << kmax) - 1ull);
+              // undecided positions of this lane's half
+              uint32_t pend = pvalid ? (uint32_t)(live64 >> (32 * hf)) : 0u;
+              uint64_t flips64 = 0ull;
+              float dEb = 0.0f;
+              const int64_t pchain = item.chain0 + cc;
+              if (L == 0) stamp(a, Gb, 9);
+    #pragma unroll 1
+              for (;;) {
+                const uint32_t lo = __reduce_min_sync(
+                    0xffffffffu, pend ? (uint32_t)(__ffs(pend) - 1) : 32u);
+                uint32_t m[4];  // bit k: position certainly rejected
+#pragma unroll
+                for (int qd = 0; qd < 4; ++qd) {
+                  m[qd] = 0u;
+                  if (8 * qd + 8 > (int)lo) {
+#pragma unroll
+                    for (int jj = 7; jj >= 0; --jj) {
+                      const int k = 8 * qd + jj;
+                      const uint32_t x = __float_as_uint((h[k] + w[k]) * w[k]);
+                      m[qd] = __funnelshift_l(x, m[qd], 1);
+                    }
+                  }
+                }
+                const uint32_t cand =
+                    ~(m[0] | (m[1] << 8) | (m[2] << 16) | (m[3] << 24)) & pend;
+                const uint32_t other = __shfl_xor_sync(0xffffffffu, cand, 16);
+                const uint32_t c0 = hf ? other : cand, c1 = hf ? cand : other;
+                if (L == 0) count(a, 2, 1);
+                if (__all_sync(0xffffffffu, (c0 | c1) == 0u)) break;
+                if ((c0 | c1) == 0u) {
+                  pend = 0u;  // the rest rejected: done
+                } else {
+                  // the chain's next decision; positions up to it decided
+                  int js;
+                  if (c0) {
+                    js = __ffs(c0) - 1;
+                    if (hf == 0) pend &= ~((2u << js) - 1u);
+                  } else {
+                    js = 32 + __ffs(c1) - 1;
+                    pend = hf == 0 ? 0u : pend & ~((2u << (js - 32)) - 1u);
+                  }
+                  const uint64_t bit = 1ull << js;
+                  // the field at decision: loaded value + this block's
+                  // earlier flips, in the order the fields took them
+                  float hj = dl_s[cidx(cc, js)];
+                  uint64_t fb = flips64;
+                  while (fb) {
+                    const int i = __ffsll((long long)fb) - 1;
+                    fb &= fb - 1ull;
+                    const uint32_t si = (i < 32 ? o0 >> i : o1 >> (i - 32)) & 1u;
+                    hj = fmaf(si ? -scale : scale, jb[i * 64 + js], hj);
+                  }
+                  const bool sbit =
+                      ((js < 32 ? o0 >> js : o1 >> (js - 32)) & 1u) != 0u;
+                  const float x = sbit ? hj : -hj;
+                  const float ak = lfb[cidx(cc, js)];
+                  const float th = fminf(
+                      fmaf(2.0f * band1, fabsf(ak), fmaf(ak, invbs, 2.0f * band0)),
+                      0.0f);
+                  bool acc = x >= th;
+                  if (!acc) {
+                    acc = metropolis_accept_lf(
+                        scale * x, pbeta, lf_of(ak),
+                        chain_seed(a.seed, a.s.stream_key, pchain),
+                        (uint32_t)inst, sweep, (uint32_t)(pchain - chain_base),
+                        (uint32_t)(i0 + js));
+                  }
+                  if (acc) {
+                    flips64 |= bit;
+                    const float dl = sbit ? -scale : scale;
+                    dEb = fmaf(dl, hj, dEb);  // dl h = -dn
+                    const float4* row =
+                        reinterpret_cast<const float4*>(jb + js * 64 + 32 * hf);
+#pragma unroll
+                    for (int q4 = 0; q4 < 8; ++q4) {
+                      const float4 v = row[q4];
+                      h[4 * q4 + 0] = fmaf(dl, v.x, h[4 * q4 + 0]);
+                      h[4 * q4 + 1] = fmaf(dl, v.y, h[4 * q4 + 1]);
+                      h[4 * q4 + 2] = fmaf(dl, v.z, h[4 * q4 + 2]);
+                      h[4 * q4 + 3] = fmaf(dl, v.w, h[4 * q4 + 3]);
+                    }
+                  }
+                }
+              }
+              if (L == 0) stamp(a, Gb, 10);
+              // this lane's half of the chain's A row, once the previous
+              // block's MMAs (which read A) are done
+              bool a_ok = true;
+              if (Gb > G0) a_ok = tc_wait(sh.mma_done, (Gb - 1) & 1, sh, status);
+              if (L == 0) stamp(a, Gb, 11);
+              const uint32_t fm = (uint32_t)(flips64 >> (32 * hf));
+              if (a_ok) {
+                const int mr = 128 - CC + cc;
+                unsigned char* rowp = smem + C::A_OFF + ((mr >> 3) * 8) * 128 +
+                                      (mr & 7) * 16;
+#pragma unroll
+                for (int kc = 0; kc < 4; ++kc)
+                  *reinterpret_cast<uint4*>(rowp + (4 * hf + kc) * 128) =
+                      make_uint4(0u, 0u, 0u, 0u);
+                const uint16_t one = ising ? 0x4000u : 0x3F80u;  // BF16 scale
+                uint32_t fb = fm;
+                while (fb) {
+                  const int j = __ffs(fb) - 1;
+                  fb &= fb - 1u;
+                  const int pj = 32 * hf + j;
+                  *reinterpret_cast<uint16_t*>(rowp + (pj >> 3) * 128 +
+                                               (pj & 7) * 2) =
+                      (uint16_t)(one | (((om >> j) & 1u) ? 0x8000u : 0u));
+                }
+              }
+              if (pvalid) {
+                spins_s[(2 * t + hf) * CC + cc] = om ^ fm;
+                if (hf == 0) dE_s[cc] += (double)dEb;
+              }
+              blk_mf = __reduce_max_sync(
+                  0xffffffffu, pvalid ? (uint32_t)__popcll(flips64) : 0u);
+              if (L == 0) count(a, 0, 1);
+              fence_proxy_async();
+            }
+          } else {
           bool go = q == qt && !*sh.abort;
           // fields of this block: the previous block's critical MMA (not
           // needed for a unit's first block or after a recompute)
