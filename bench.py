@@ -1238,11 +1238,19 @@ def main():
         terms = batch.tc_terms
         alg = 2.0 * C * n * n * terms
         fold = 1 if n <= 512 else (2 if n <= 1024 else 4)
+        fp8 = bool(getattr(batch, "tc_fp8", False))
+        # E4M3 tiles run kind::f8f6f4 MMAs: no measured FP8 peak exists, so
+        # the denominator is twice the measured BF16 one (the nominal dense
+        # FP8 : BF16 ratio, 4.5 : 2.25 PFLOP/s)
+        peak = 2.0 * bf16 if fp8 else bf16
         roof = {"bound": "tensor", "achieved": alg / sweep_s / 1e12,
-                "peak": bf16, "unit": "TFLOP/s",
-                "frac": alg / sweep_s / 1e12 / bf16, "traffic": None,
-                "peak_source": peak_kind + " (bf16 burst)",
-                "kernel": f"k_sweep_tc<{fold}>", "bf16_terms": terms,
+                "peak": peak, "unit": "TFLOP/s",
+                "frac": alg / sweep_s / 1e12 / peak, "traffic": None,
+                "peak_source": peak_kind + (
+                    " (2 x bf16 burst: nominal fp8/bf16 ratio)" if fp8
+                    else " (bf16 burst)"),
+                "kernel": f"k_sweep_tc<{fold}{', e4m3' if fp8 else ''}>",
+                "tile_format": "e4m3" if fp8 else "bf16", "bf16_terms": terms,
                 "issued_flop_per_launch": alg * fold,
                 "alg_flop_per_launch": alg, "sweep_ms": sweep_s * 1e3}
         tp = os.path.join(ROOT, "profiles",
@@ -1341,8 +1349,11 @@ def main():
                        "kernel_choice": args.kernel,
                        "tc_min_n": batch.tc_min_n,
                        "kernel": ("persistent tensor-core blocked sweep "
-                                  "(tcgen05, split-BF16%s)" %
-                                  (", exchange fused" if fused else ""))
+                                  "(tcgen05, %s%s)" %
+                                  ("E4M3 tiles" if getattr(batch, "tc_fp8",
+                                                           False)
+                                   else "split-BF16",
+                                   ", exchange fused" if fused else ""))
                                  if use_tc else
                                  "plain local-field sweep (CUDA cores)"},
             "roofline": roof,

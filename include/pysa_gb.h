@@ -218,6 +218,12 @@ typedef struct {
    * item-sweeps evenly over the CTAs (wrap-around units) instead of running
    * fixed-length units from a queue. */
   int32_t tc_uniform;
+  /* caller, read by pysa_gb_tc_setup: 1 = the tensor-core tiles in FP8 E4M3
+   * (half the bytes and MMA instructions of BF16; results identical).  Only
+   * valid when every tensor-core instance's couplings are exact in E4M3
+   * (integers up to 16 in magnitude, for instance) and tc_terms = 1; random
+   * visiting order keeps BF16 tiles. */
+  int32_t tc_fp8;
 } pysa_gb_workspace;
 
 /* Host copies of the per-instance tables, used to plan the work list. */

@@ -55,7 +55,7 @@ class Workspace(ctypes.Structure):
                 ("csr_item_count", I32), ("csr_width", I32),
                 ("csr_chains", I32), ("wide_item_start", I32),
                 ("wide_item_count", I32), ("tc_item_chains", I32),
-                ("tc_uniform", I32)]
+                ("tc_uniform", I32), ("tc_fp8", I32)]
 
 
 class HostTables(ctypes.Structure):

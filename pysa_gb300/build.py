@@ -24,7 +24,8 @@ if os.environ.get("PYSA_GB_TRACE") == "1":  # timeline stamps (diagnostics)
     FLAGS.append("-DPYSA_GB_TRACE")
 
 SOURCES = ["abi.cu", "kernels_aux.cu", "plain_small.cu", "plain_large.cu",
-           "ais.cu", "sweep_tc.cu", "sweep_csr.cu", "sweep_wide.cu", "noalloc.cu",
+           "ais.cu", "sweep_tc.cu", "sweep_tc_e8.cu", "sweep_csr.cu",
+           "sweep_wide.cu", "noalloc.cu",
            "gemm_tc.cu", "mlp.cu"]
 
 

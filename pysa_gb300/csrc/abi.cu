@@ -474,6 +474,8 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   std::vector<TcItem> items;
   if (ws->tc_item_chains < 0)
     return fail(PYSA_GB_ERR_ARG, "tc_item_chains must be >= 0");
+  if (ws->tc_fp8 && ws->tc_terms != 1)
+    return fail(PYSA_GB_ERR_ARG, "tc_fp8 needs tc_terms = 1");
   const std::vector<int> isz =
       tc_item_sizes(p->num_instances, host, min_n, ws->tc_item_chains);
   const int folds[3] = {1, 2, 4};
@@ -517,7 +519,8 @@ int pysa_gb_tc_setup(const pysa_gb_problems* p, const pysa_gb_host_tables* host,
   for (int i = 0; i < p->num_instances; ++i) {
     if (!flags[i]) continue;
     cudaError_t e = launch_pack_tc(p->J + host->j_off[i], host->ld[i],
-                                   host->n[i], ws->tc_terms, ws->tc_b + boff[i],
+                                   host->n[i], ws->tc_terms, ws->tc_fp8 != 0,
+                                   ws->tc_b + boff[i],
                                    ws->tc_diag + doff[i], st);
     if (e != cudaSuccess) return cuda_fail(e, "pack tc tiles");
   }
@@ -665,7 +668,7 @@ int pysa_gb_sweeps(const pysa_gb_problems* p, pysa_gb_state* s,
   ta.decision_mode = g_decision_mode;
   ta.round_limit = g_round_limit;
   ta.wrap = 0;
-  ta.pad_wrap_ = 0;
+  ta.e8 = ws->tc_fp8 != 0;
   ta.sched = ws->tc_sched;
   ta.perm = ws->perm;
   ta.perm_slots = a.perm_slots;

@@ -28,6 +28,8 @@
 // precompute the next block's log-uniforms.  Every wait is bounded; a
 // timeout sets the status word and an abort flag that releases every other
 // wait.
+#include <cuda_fp8.h>
+
 #include "aux.cuh"
 #include "tc_api.h"
 #include "tc_ptx.cuh"
@@ -45,15 +47,24 @@ constexpr int kTW = 256;
 
 // RND: random visiting order (one permutation per instance and sweep); the
 // B ring keeps two stages to make room for the gathered block fields.
-template <int F, bool RND = false>
+// E8: operands in FP8 E4M3 (couplings exact in E4M3; deltas 0, +-1, +-2):
+// half the bytes per row, so twice the ring stages in the same space.
+template <int F, bool RND = false, bool E8 = false>
 struct TcCfg {
   static constexpr int CC = 128 / F;          // chains per CTA
-  static constexpr int NS = (F == 1 || RND) ? 2 : 3;   // B ring stages
+  static constexpr int NS = E8 ? (F == 1 ? 4 : F == 2 ? 6 : 8)
+                               : ((F == 1 || RND) ? 2 : 3);  // B ring stages
   static constexpr int WORDS = 16 * F;        // spin words per chain
+  // operand rows: K = 64 elements = ROW_B bytes, in 16-byte chunks of the
+  // canonical no-swizzle K-major layout: core matrices of 8 rows x 16
+  // bytes, K-adjacent ones 128 bytes apart, 8-row groups SBO bytes apart
+  static constexpr int ROW_B = E8 ? 64 : 128;
+  static constexpr int CPR = ROW_B / 16;      // chunks per row
+  static constexpr uint32_t SBO = 8u * ROW_B;
   // A operand: ONE copy of the CC chains' delta rows (physical rows
   // 128 - CC ... 127) with 128 - CC zero rows on either side; slice q's
   // 128-row MMA operand starts (128 - CC - q CC) rows in, so only its own
-  // chains' rows fall on its lanes.  K = 64 BF16 = 128 bytes per row.
+  // chains' rows fall on its lanes.
   // fold 4: two A buffers (block t writes buffer t & 1 while the MMAs of
   // block t - 1 still read the other), interleaved with the zero rows:
   // [zero][buffer 0][zero][buffer 1][zero]; buffer b's delta rows are
@@ -62,9 +73,9 @@ struct TcCfg {
   static constexpr int A_ROWS =
       F == 1 ? 128 : (A_NBUF == 2 ? 384 - CC : 256 - CC);
   static constexpr size_t A_OFF = 0;
-  static constexpr size_t A_BYTES = (size_t)A_ROWS * 128;
+  static constexpr size_t A_BYTES = (size_t)A_ROWS * ROW_B;
   static constexpr size_t B_OFF = A_OFF + A_BYTES;
-  static constexpr size_t B_STAGE = (size_t)kTW * 128;  // one tile
+  static constexpr size_t B_STAGE = (size_t)kTW * ROW_B;  // one tile
   static constexpr size_t JBB_OFF = B_OFF + NS * B_STAGE;
   static constexpr size_t SPIN_OFF = JBB_OFF + 2 * 16384;
   // log-uniforms of a block: two buffers of [chain][64] floats in the
@@ -250,6 +261,14 @@ __device__ __forceinline__ uint32_t bf16_bits(float d) {
   return __float_as_uint(d) >> 16;
 }
 
+// E4M3 bits of d in {0, +-1, +-2} (exponent bias 7, three mantissa bits:
+// 1 = 0x38, 2 = 0x40, sign 0x80); zero of either sign is 0.
+__device__ __forceinline__ uint32_t e4m3_bits(float d) {
+  const uint32_t u = __float_as_uint(d);
+  if ((u & 0x7FFFFFFFu) == 0u) return 0u;
+  return ((((u >> 23) & 0xFFu) - 120u) << 3) | ((u >> 24) & 0x80u);
+}
+
 // The rare exact redo of one deciding thread's sub-block (some decision of
 // the warp fell inside the f32 band), kept out of line: inlined, its code
 // and registers slow the fast path by about 12 %.  It rebuilds the
@@ -400,9 +419,9 @@ __device__ __forceinline__ bool wrap_piece(int items, int S, int m, int k,
 // work from the queue earlier (so is running) owns, so the wait always ends.
 // Within a unit the fields stay in TMEM across sweeps; the replica exchange
 // of the item's reads runs in the kernel when fused.
-template <int F, bool RND>
+template <int F, bool RND, bool E8>
 __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
-  using C = TcCfg<F, RND>;
+  using C = TcCfg<F, RND, E8>;
   constexpr int CC = C::CC;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + C::BAR_OFF);
@@ -452,6 +471,20 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   float* ex_E2 = dl_s + 21 * CC;
   float* ex_D = dl_s + 25 * CC;
   const uint32_t smem_base = smem_addr(smem);
+  // A operand: physical row m, and the element of position j (< 64) of a
+  // row set to +-1 (QUBO) or +-2 (Ising) deltas
+  auto a_row = [&](int m) {
+    return smem + C::A_OFF + ((m >> 3) * C::CPR) * 128 + (m & 7) * 16;
+  };
+  const bool ising_ = a.p.problem_type == PYSA_GB_ISING;
+  auto a_put = [&](unsigned char* rowp, int j, bool neg) {
+    if constexpr (E8)
+      rowp[(j >> 4) * 128 + (j & 15)] =
+          (unsigned char)((ising_ ? 0x40u : 0x38u) | (neg ? 0x80u : 0u));
+    else
+      *reinterpret_cast<uint16_t*>(rowp + (j >> 3) * 128 + (j & 7) * 2) =
+          (uint16_t)((ising_ ? 0x4000u : 0x3F80u) | (neg ? 0x8000u : 0u));
+  };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int32_t* status = a.s.status;
@@ -479,7 +512,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *sh.tmem_slot;
-  const uint32_t idesc_full = tc::idesc_bf16(128, kTW);
+  const uint32_t idesc_full =
+      E8 ? tc::idesc_e4m3(128, kTW) : tc::idesc_bf16(128, kTW);
 
   // decision-thread identity: TMEM lane L = slice q, chain c
   const int L = threadIdx.x;
@@ -660,22 +694,25 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               const uint32_t w0 = spins_s[(2 * t) * CC + c];
               const uint32_t w1 = spins_s[(2 * t + 1) * CC + c];
               const int kmax = n - 64 * t < 64 ? n - 64 * t : 64;
-              uint32_t pk[32];
+              uint32_t pk[C::ROW_B / 4];
 #pragma unroll
               for (int k = 0; k < 64; ++k) {
                 const bool sb =
                     k < 32 ? ((w0 >> k) & 1u) : ((w1 >> (k - 32)) & 1u);
                 const float v = (!valid || k >= kmax) ? 0.0f
                                 : sb ? 1.0f : (ising ? -1.0f : 0.0f);
-                const uint32_t b16 = bf16_bits(v);
-                if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
+                if constexpr (E8) {
+                  const uint32_t b8 = e4m3_bits(v) << (8 * (k & 3));
+                  if (k & 3) pk[k >> 2] |= b8; else pk[k >> 2] = b8;
+                } else {
+                  const uint32_t b16 = bf16_bits(v);
+                  if (k & 1) pk[k >> 1] |= b16 << 16; else pk[k >> 1] = b16;
+                }
               }
               {
-                const int m = 128 - CC + c;  // chain c's physical A row
-                unsigned char* rowp = smem + C::A_OFF +
-                                      ((m >> 3) * 8) * 128 + (m & 7) * 16;
+                unsigned char* rowp = a_row(128 - CC + c);  // chain c's row
 #pragma unroll
-                for (int kc = 0; kc < 8; ++kc)
+                for (int kc = 0; kc < C::CPR; ++kc)
                   *reinterpret_cast<uint4*>(rowp + kc * 128) =
                       make_uint4(pk[4 * kc], pk[4 * kc + 1], pk[4 * kc + 2],
                                  pk[4 * kc + 3]);
@@ -971,22 +1008,17 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               if (L == 0) stamp(a, Gb, 11);
               const uint32_t fm = (uint32_t)(flips64 >> (32 * hf));
               if (a_ok) {
-                const int mr = 128 - CC + cc;
-                unsigned char* rowp = smem + C::A_OFF + ((mr >> 3) * 8) * 128 +
-                                      (mr & 7) * 16;
+                unsigned char* rowp = a_row(128 - CC + cc);
 #pragma unroll
-                for (int kc = 0; kc < 4; ++kc)
-                  *reinterpret_cast<uint4*>(rowp + (4 * hf + kc) * 128) =
+                for (int kc = 0; kc < C::CPR / 2; ++kc)
+                  *reinterpret_cast<uint4*>(rowp +
+                                            (C::CPR / 2 * hf + kc) * 128) =
                       make_uint4(0u, 0u, 0u, 0u);
-                const uint16_t one = ising ? 0x4000u : 0x3F80u;  // BF16 scale
                 uint32_t fb = fm;
                 while (fb) {
                   const int j = __ffs(fb) - 1;
                   fb &= fb - 1u;
-                  const int pj = 32 * hf + j;
-                  *reinterpret_cast<uint16_t*>(rowp + (pj >> 3) * 128 +
-                                               (pj & 7) * 2) =
-                      (uint16_t)(one | (((om >> j) & 1u) ? 0x8000u : 0u));
+                  a_put(rowp, 32 * hf + j, ((om >> j) & 1u) != 0u);
                 }
               }
               if (pvalid) {
@@ -1022,17 +1054,27 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
           // one sub-block's deltas of chain c into its A row (one copy,
           // seen by every slice's MMA)
           auto put_a = [&](int gg, const float* d) {
-            uint32_t pkg[8];
+            unsigned char* rowp = a_row(
+                128 - CC + c + (C::A_NBUF == 2 ? 128 * (int)(Gb & 1) : 0));
+            if constexpr (E8) {
+              uint32_t pkg[4];
 #pragma unroll
-            for (int j = 0; j < 16; j += 2)
-              pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
-            const int m = 128 - CC + c + (C::A_NBUF == 2 ? 128 * (int)(Gb & 1) : 0);
-            unsigned char* rowp = smem + C::A_OFF + ((m >> 3) * 8) * 128 +
-                                  (m & 7) * 16;
-            *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
-                make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
-            *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
-                make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
+              for (int j = 0; j < 16; j += 4)
+                pkg[j >> 2] = e4m3_bits(d[j]) | (e4m3_bits(d[j + 1]) << 8) |
+                              (e4m3_bits(d[j + 2]) << 16) |
+                              (e4m3_bits(d[j + 3]) << 24);
+              *reinterpret_cast<uint4*>(rowp + gg * 128) =
+                  make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+            } else {
+              uint32_t pkg[8];
+#pragma unroll
+              for (int j = 0; j < 16; j += 2)
+                pkg[j >> 1] = bf16_bits(d[j]) | (bf16_bits(d[j + 1]) << 16);
+              *reinterpret_cast<uint4*>(rowp + (2 * gg) * 128) =
+                  make_uint4(pkg[0], pkg[1], pkg[2], pkg[3]);
+              *reinterpret_cast<uint4*>(rowp + (2 * gg + 1) * 128) =
+                  make_uint4(pkg[4], pkg[5], pkg[6], pkg[7]);
+            }
           };
           if (go) {
             tc::fence_after_sync();
@@ -1297,23 +1339,18 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               }
               if (lead) stamp(a, Gb, 11);
               if (a_ok) {
-                const int m = 128 - CC + c +
-                              (C::A_NBUF == 2 ? 128 * (int)(Gb & 1) : 0);
-                unsigned char* rowp = smem + C::A_OFF + ((m >> 3) * 8) * 128 +
-                                      (m & 7) * 16;
+                unsigned char* rowp = a_row(
+                    128 - CC + c + (C::A_NBUF == 2 ? 128 * (int)(Gb & 1) : 0));
 #pragma unroll
-                for (int kc = 0; kc < 8; ++kc)
+                for (int kc = 0; kc < C::CPR; ++kc)
                   *reinterpret_cast<uint4*>(rowp + kc * 128) =
                       make_uint4(0u, 0u, 0u, 0u);
-                const uint16_t one = ising ? 0x4000u : 0x3F80u;  // BF16 scale
                 uint64_t fb = flips64;
                 while (fb) {
                   const int j = __ffsll((long long)fb) - 1;
                   fb &= fb - 1ull;
                   const uint32_t sj = (j < 32 ? o0 >> j : o1 >> (j - 32)) & 1u;
-                  *reinterpret_cast<uint16_t*>(rowp + (j >> 3) * 128 +
-                                               (j & 7) * 2) =
-                      (uint16_t)(one | (sj ? 0x8000u : 0u));
+                  a_put(rowp, j, sj != 0u);
                 }
               }
             } else {
@@ -1731,25 +1768,35 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
         auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi,
                             uint32_t acc, int ab) {
           if (r_hi <= r_lo) return;
-          const uint32_t idesc = r_hi - r_lo == kTW
-                                     ? idesc_full
-                                     : tc::idesc_bf16(128, r_hi - r_lo);
+          const uint32_t idesc =
+              r_hi - r_lo == kTW
+                  ? idesc_full
+                  : (E8 ? tc::idesc_e4m3(128, r_hi - r_lo)
+                        : tc::idesc_bf16(128, r_hi - r_lo));
           // slice qq's view: 128 rows starting (128 - CC - qq CC) rows in
           const uint32_t a0 =
               smem_base +
               (uint32_t)(C::A_OFF +
-                         (size_t)((128 - CC - qq * CC + 128 * ab) >> 3) * 1024);
+                         (size_t)((128 - CC - qq * CC + 128 * ab) >> 3) * C::SBO);
           const uint32_t b0 = smem_base +
                               (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
-                              (uint32_t)(r_lo / 8) * 1024u;
-          // K steps of 16 are 256 bytes apart: 16 in the descriptors'
-          // address field (shared addresses stay below 2^18)
-          const uint64_t ad = tc::smem_desc(a0, 128, 1024);
-          const uint64_t bd = tc::smem_desc(b0, 128, 1024);
+                              (uint32_t)(r_lo / 8) * C::SBO;
+          // K steps (16 BF16 or 32 E4M3 elements: two core matrices) are
+          // 256 bytes apart: 16 in the descriptors' address field (shared
+          // addresses stay below 2^18)
+          const uint64_t ad = tc::smem_desc(a0, 128, C::SBO);
+          const uint64_t bd = tc::smem_desc(b0, 128, C::SBO);
+          if constexpr (E8) {
 #pragma unroll
-          for (int ks = 0; ks < 4; ++ks)
-            tc::mma_bf16(taddr + kTW * j + r_lo, ad + 16u * ks, bd + 16u * ks,
-                         idesc, (acc | (uint32_t)ks) ? 1u : 0u);
+            for (int ks = 0; ks < 2; ++ks)
+              tc::mma_e4m3(taddr + kTW * j + r_lo, ad + 16u * ks,
+                           bd + 16u * ks, idesc, (acc | (uint32_t)ks) ? 1u : 0u);
+          } else {
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks)
+              tc::mma_bf16(taddr + kTW * j + r_lo, ad + 16u * ks,
+                           bd + 16u * ks, idesc, (acc | (uint32_t)ks) ? 1u : 0u);
+          }
         };
         bool ok = true;
         for (int s = 0; s < KU && ok; ++s) {
@@ -1858,7 +1905,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
       if (lane == 0) {
         const uint16_t* Bp = a.tc_b + item.b_off;
         const float* D = a.tc_diag + item.diag_off;
-        const size_t tile_elems = (size_t)kTW * 64;
+        const size_t tile_bytes = (size_t)kTW * C::ROW_B;
         // diagonal block of global block Gx (block (Gx - G0) % NB of the
         // unit) into buffer Gx & 1, once block Gx - 2 has released it
         // random order: the sweep's repacked slot (same offsets)
@@ -1889,10 +1936,11 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             return false;
           const int width = S - kTW * j < kTW ? S - kTW * j : kTW;
           const size_t src =
-              ((((size_t)t * T + term) * F + qq) * NT + j) * tile_elems;
-          const uint32_t bytes = (uint32_t)width * 128;
+              ((((size_t)t * T + term) * F + qq) * NT + j) * tile_bytes;
+          const uint32_t bytes = (uint32_t)width * C::ROW_B;
           mbar_expect_tx_arrive(&sh.full[slot], bytes);
-          bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE, Bsrc + src, bytes,
+          bulk_g2s(smem + C::B_OFF + slot * C::B_STAGE,
+                   reinterpret_cast<const unsigned char*>(Bsrc) + src, bytes,
                    &sh.full[slot]);
           ++u;
           return true;
@@ -2067,6 +2115,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   }
 }
 
+#ifndef PYSA_GB_TC_E8_UNIT
 // -------------------------------------------------------------- packing
 // B tiles: for block t, term, slice qq, tile j: rows r < width (column
 // qq*S + kTW j + r), k < 64 (spin 64 t + k), canonical no-swizzle K-major
@@ -2099,6 +2148,35 @@ __global__ void k_pack_tc_b(const float* Jt, int ld, int n, int F, int terms,
     const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
     const __nv_bfloat16 o = term == 0 ? hi : lo;
     out[e] = *reinterpret_cast<const uint16_t*>(&o);
+  }
+}
+
+// E4M3 tiles (one term, couplings exact in E4M3): the same tiles with
+// 16-byte core-matrix rows of 16 elements, ((r / 8) * 4 + k / 16) * 128 +
+// (r % 8) * 16 + k % 16 (bytes).
+__global__ void k_pack_tc_b8(const float* Jt, int ld, int n, int F,
+                             unsigned char* out) {
+  const int NP = (n + 64 * F - 1) / (64 * F) * (64 * F);
+  const int S = NP / F, NB = (n + 63) / 64, NT = (S + kTW - 1) / kTW;
+  const int64_t tile = (int64_t)kTW * 64;
+  const int64_t total = (int64_t)NB * F * NT * tile;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rest = e;
+    const int within = (int)(rest % tile);
+    rest /= tile;
+    const int j = (int)(rest % NT);
+    rest /= NT;
+    const int qq = (int)(rest % F);
+    const int t = (int)(rest / F);
+    const int cm = within / 128, inside = within % 128;
+    const int r = (cm / 4) * 8 + inside / 16;
+    const int k = (cm % 4) * 16 + inside % 16;
+    const int row = 64 * t + k, col = qq * S + kTW * j + r;
+    float v = 0.0f;
+    if (row < n && col < n && r < kTW && kTW * j + r < S)
+      v = Jt[(int64_t)row * ld + col];
+    out[e] = (unsigned char)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
   }
 }
 
@@ -2208,12 +2286,17 @@ int64_t tc_b_elems(int n, int terms) {
 int64_t tc_diag_elems(int n) { return (int64_t)((n + 63) / 64) * 4096; }
 
 cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
-                           uint16_t* b_out, float* diag_out, cudaStream_t st) {
+                           bool e8, uint16_t* b_out, float* diag_out,
+                           cudaStream_t st) {
   const int F = tc_fold_for(n);
   int64_t tb = tc_b_elems(n, terms);
   int blocks = (int)((tb + 255) / 256);
   if (blocks > 8192) blocks = 8192;
-  k_pack_tc_b<<<blocks, 256, 0, st>>>(Jt, ld, n, F, terms, b_out);
+  if (e8)
+    k_pack_tc_b8<<<blocks, 256, 0, st>>>(
+        Jt, ld, n, F, reinterpret_cast<unsigned char*>(b_out));
+  else
+    k_pack_tc_b<<<blocks, 256, 0, st>>>(Jt, ld, n, F, terms, b_out);
   int64_t td = tc_diag_elems(n);
   blocks = (int)((td + 255) / 256);
   if (blocks > 8192) blocks = 8192;
@@ -2221,34 +2304,53 @@ cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
   return cudaGetLastError();
 }
 
-template <int F, bool RND>
+#endif  // PYSA_GB_TC_E8_UNIT
+
+template <int F, bool RND, bool E8>
 static cudaError_t launch_tc_t(const TcArgs& a, int count, cudaStream_t st) {
+  using C = TcCfg<F, RND, E8>;
   static bool attr_set[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !attr_set[dev]) {
     cudaError_t e = cudaFuncSetAttribute(
-        k_sweep_tc<F, RND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)TcCfg<F, RND>::BYTES);
+        k_sweep_tc<F, RND, E8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)C::BYTES);
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
-  k_sweep_tc<F, RND><<<count, 256, TcCfg<F, RND>::BYTES, st>>>(a);
+  k_sweep_tc<F, RND, E8><<<count, 256, C::BYTES, st>>>(a);
   return cudaGetLastError();
 }
+
+#ifdef PYSA_GB_TC_E8_UNIT
+// The E4M3 variants, compiled in their own translation unit
+// (sweep_tc_e8.cu) in parallel with the BF16 ones.
+cudaError_t launch_tc_e8(const TcArgs& a, int F, int count, cudaStream_t st) {
+  switch (F) {
+    case 1: return launch_tc_t<1, false, true>(a, count, st);
+    case 2: return launch_tc_t<2, false, true>(a, count, st);
+    case 4: return launch_tc_t<4, false, true>(a, count, st);
+  }
+  return cudaErrorInvalidValue;
+}
+#else
+cudaError_t launch_tc_e8(const TcArgs& a, int F, int count, cudaStream_t st);
 
 cudaError_t launch_tc(const TcArgs& a, int F, bool random, int max_ctas,
                       cudaStream_t st) {
   const int64_t units = (int64_t)a.num_items * a.units_per_item;
   if (units <= 0) return cudaSuccess;
   const int count = (int)(units < max_ctas ? units : max_ctas);
+  // E4M3 tiles in visiting order only (random order repacks BF16 tiles)
+  if (a.e8 && !random) return launch_tc_e8(a, F, count, st);
   switch (F * 2 + (random ? 1 : 0)) {
-    case 2: return launch_tc_t<1, false>(a, count, st);
-    case 3: return launch_tc_t<1, true>(a, count, st);
-    case 4: return launch_tc_t<2, false>(a, count, st);
-    case 5: return launch_tc_t<2, true>(a, count, st);
-    case 8: return launch_tc_t<4, false>(a, count, st);
-    case 9: return launch_tc_t<4, true>(a, count, st);
+    case 2: return launch_tc_t<1, false, false>(a, count, st);
+    case 3: return launch_tc_t<1, true, false>(a, count, st);
+    case 4: return launch_tc_t<2, false, false>(a, count, st);
+    case 5: return launch_tc_t<2, true, false>(a, count, st);
+    case 8: return launch_tc_t<4, false, false>(a, count, st);
+    case 9: return launch_tc_t<4, true, false>(a, count, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -2257,5 +2359,6 @@ int tc_chains_per_cta(int n) {
   const int F = tc_fold_for(n);
   return F > 0 ? 128 / F : 0;
 }
+#endif  // PYSA_GB_TC_E8_UNIT
 
 }  // namespace pysa_gb

@@ -29,7 +29,7 @@ struct TcArgs {
   int32_t unit_sweeps;      // sweeps per work unit (wrap: of the launch)
   int32_t units_per_item;   // work units per item in this launch (wrap: 1)
   int32_t wrap;             // 1: wrap-around units (items of one size)
-  int32_t pad_wrap_;
+  int32_t e8;               // 1: tiles in E4M3 (visiting order only)
   int32_t fuse_exchange;    // 1: exchange inside the kernel (R | chains/CTA)
   int32_t use_pt;
   int32_t advance_counter;  // 1: the last CTA advances the sweep counter
@@ -59,8 +59,11 @@ int tc_fold_for(int n);  // 1, 2, 4 or -1 (n > 2048)
 int tc_chains_per_cta(int n);
 int64_t tc_b_elems(int n, int terms);
 int64_t tc_diag_elems(int n);
+// e8: one term in E4M3 (every coupling exact in E4M3), in the first half of
+// the BF16 tiles' space.
 cudaError_t launch_pack_tc(const float* Jt, int ld, int n, int terms,
-                           uint16_t* b_out, float* diag_out, cudaStream_t st);
+                           bool e8, uint16_t* b_out, float* diag_out,
+                           cudaStream_t st);
 // Persistent launch over a.num_items * a.units_per_item work units with at
 // most `max_ctas` CTAs (wrap: min(num_items, max_ctas) CTAs, one share of
 // the item-sweeps each); a.sched must hold 2 + num_items zeroed words.

@@ -227,6 +227,25 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_taddr, uint64_t a_desc,
       : "memory");
 }
 
+// Instruction descriptor, kind::f8f6f4: D f32, A and B E4M3 (format 0),
+// both K-major; N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T with E4M3 operands (K = 32 per
+// instruction), issued by one thread.
+__device__ __forceinline__ void mma_e4m3(uint32_t d_taddr, uint64_t a_desc,
+                                         uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d_taddr),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // Arrive on an mbarrier once every tcgen05 operation issued so far by this
 // thread has completed.
 __device__ __forceinline__ void commit(uint64_t* bar) {

@@ -51,6 +51,20 @@ def bf16_exact(a: np.ndarray) -> bool:
     return bool(np.all((u & 0xFFFF) == 0))
 
 
+def e4m3_exact(a: np.ndarray) -> bool:
+    """True when every value is exactly representable in FP8 E4M3 (four
+    exponent bits, bias 7, three mantissa bits, largest finite 448): zero,
+    multiples of 2^-9 below 2^-6, and above it values whose float32
+    mantissa keeps only its top three bits."""
+    x = np.abs(np.ascontiguousarray(a, np.float32))
+    if not np.all(np.isfinite(x)) or x.max(initial=0.0) > 448.0:
+        return False
+    small = x < 2.0 ** -6
+    sub_ok = np.all(np.mod(x[small] * 2.0 ** 9, 1.0) == 0.0)
+    u = x[~small].view(np.uint32)
+    return bool(sub_ok and np.all((u & 0xFFFFF) == 0))
+
+
 def csr_tables(J: np.ndarray):
     """Sparse-row tables of a dense coupling matrix, as the sparse-row sweep
     reads them: row i of J^T (the row every kernel reads for spin i) keeps
@@ -141,7 +155,8 @@ class PTBatch:
     def __init__(self, problem_type: str, instances: list[Instance],
                  device: torch.device | str | None = None,
                  perm_slots: int = 1, kernel: str = "auto",
-                 tc_terms: int | None = None, sparse=None):
+                 tc_terms: int | None = None, sparse=None,
+                 tc_fp8: bool = False):
         """kernel: 'plain' (CUDA-core sweep for every instance), 'tc'
         (tensor-core blocked sweep for every instance, sequential order,
         64 <= n <= 2048), 'auto' (tensor cores for the instances with
@@ -154,13 +169,16 @@ class PTBatch:
         (field of spin i from row i's nonzero couplings, O(degree) per
         attempt): None / False for none, True for all, 'auto' for those
         whose mean degree is at most max(8, n / 64), or one bool per
-        instance."""
+        instance.  tc_fp8: tensor-core tiles in FP8 E4M3 when every dense
+        J is exact in E4M3 and one BF16 term suffices (BF16 otherwise); the
+        results are the same either way."""
         if not torch.cuda.is_available():
             raise RuntimeError(
                 "pysa_gb300 needs a CUDA GPU: the sweeps run only as "
                 "sm_103a kernels (no CPU path)")
         self.lib = _lib.load()
         self._tc_terms_req = tc_terms
+        self._tc_fp8_req = tc_fp8
         self.device = torch.device(device or "cuda")
         self.problem_type = problem_type
         self.ptype = _lib.ISING if problem_type == "ising" else _lib.QUBO
@@ -376,6 +394,11 @@ class PTBatch:
             self.ws.tc_terms = terms
             self.tc_terms = terms
             self._tc_terms_cap = terms
+            fp8 = bool(self._tc_fp8_req) and terms == 1 and all(
+                e4m3_exact(_dense(x.J)) for i, x in enumerate(self.instances)
+                if not self.sparse[i])
+            self.ws.tc_fp8 = int(fp8)
+            self.tc_fp8 = fp8
         self.ws.tc_min_n = int(min_n)
         if item_chains is not None:
             self.ws.tc_item_chains = int(item_chains)
@@ -519,8 +542,8 @@ class PTBatch:
         """Couplings and fields of instance `inst` from a dense symmetric
         problem matrix in device memory, split on the device as
         pysa/sa.py:66-69 does; the kernels' packed copies of J are rebuilt
-        on the device.  Only the BF16-exactness flag of P (one byte) comes
-        to the host."""
+        on the device.  Only the BF16- and E4M3-exactness flags of P (a
+        byte each) come to the host."""
         n = int(self.n[inst])
         P = P.detach().to(device=self.device, dtype=torch.float32)
         if P.shape != (n, n):
@@ -540,6 +563,12 @@ class PTBatch:
                                  "the batch with tc_terms=2")
             self.ws.tc_terms = terms
             self.tc_terms = terms
+            # E4M3 tiles only while every instance's couplings stay exact
+            # (checked on the device: one more byte to the host)
+            fp8 = bool(self.tc_fp8 and terms == 1 and bool(
+                (P.to(torch.float8_e4m3fn).to(torch.float32) == P).all()))
+            self.ws.tc_fp8 = int(fp8)
+            self.tc_fp8 = fp8
             check(self.lib.pysa_gb_tc_setup(ref(self.p), ref(self._ht),
                                             ref(self.ws), st), "tc setup")
         self._graphs = {}

@@ -113,6 +113,28 @@ def test_schedule_knobs_validate_without_gpu():
     assert lib.pysa_gb_set_tc_max_ctas(0) == 0
 
 
+def test_e4m3_exactness_matches_torch_conversion():
+    """The host check that selects FP8 E4M3 tiles agrees with a round trip
+    through torch's float8_e4m3fn on integers, subnormals, the largest
+    finite value and values just outside each range."""
+    import torch
+    from pysa_gb300.engine import e4m3_exact
+    rng = np.random.default_rng(3)
+    vals = np.concatenate([
+        np.arange(-20, 21), [448, 480, 464, 2 ** -9, 3 * 2 ** -9, 2 ** -10,
+                             2 ** -6, 1.0625, 1.125, 0.3, 1e-3],
+        rng.normal(size=300) * 8, rng.integers(-16, 17, 50) / 8.0,
+    ]).astype(np.float32)
+    for v in vals:
+        a = np.array([v], np.float32)
+        want = bool((torch.from_numpy(a).to(torch.float8_e4m3fn)
+                     .to(torch.float32).numpy() == a).all())
+        assert e4m3_exact(a) == want, v
+    assert e4m3_exact(np.triu(rng.integers(-16, 17, (64, 64)), 1)
+                      .astype(np.float32))
+    assert not e4m3_exact(np.array([[0.0, np.inf]], np.float32))
+
+
 def test_pack_unpack_roundtrip():
     from pysa_gb300.engine import pack_spins, unpack_spins
     rng = np.random.default_rng(0)

@@ -25,6 +25,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 SCHEDULES = ["per_item", "wrap2", "fixed8"]
+# tile formats: integer couplings |J| <= 16 are exact in FP8 E4M3 (the
+# default for them) and in BF16
+FORMATS = ["e4m3", "bf16"]
 
 
 @pytest.fixture
@@ -66,9 +69,11 @@ def _check_equal(got, want, Rd, R, n, ptype):
     assert (bs == want["best_spins"]).all(), "best spins"
 
 
-def _fused_batch(ptype, J, h, betas, Rd, fold):
+def _fused_batch(ptype, J, h, betas, Rd, fold, fmt="e4m3"):
     from pysa_gb300 import Instance, PTBatch
-    b = PTBatch(ptype, [Instance(J, h, betas, Rd)], kernel="tc")
+    b = PTBatch(ptype, [Instance(J, h, betas, Rd)], kernel="tc",
+                tc_fp8=fmt == "e4m3")
+    assert b.tc_fp8 == (fmt == "e4m3") and b.ws.tc_fp8 == b.tc_fp8
     # the path under test: every instance on the tensor cores at this fold,
     # exchange fused into the kernel
     v = {1: 0, 2: 1, 4: 2}[fold]
@@ -81,7 +86,8 @@ def _fused_batch(ptype, J, h, betas, Rd, fold):
 
 
 def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
-                   fold, graph_chunk=128, knobs=None, schedule="per_item"):
+                   fold, graph_chunk=128, knobs=None, schedule="per_item",
+                   fmt="e4m3"):
     """plan: the sweep counts of consecutive run() calls on one batch (each
     call continues the previous one's chains, as Solver resumes)."""
     from pysa_gb300 import pack_spins
@@ -94,7 +100,7 @@ def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
         x0 = (2 * rng.integers(0, 2, (Rd, R, n)) - 1).astype(np.float32)
     e0 = np.array([[oracle.energy64(J, h, s) for s in r] for r in x0],
                   np.float32)
-    b = _fused_batch(ptype, J, h, betas, Rd, fold)
+    b = _fused_batch(ptype, J, h, betas, Rd, fold, fmt)
     if knobs is not None:
         knobs(b, schedule)
     if schedule != "fixed8":
@@ -117,16 +123,17 @@ def _run_vs_oracle(oracle, ptype, n, R, Rd, tmin, tmax, plan, seed,
     assert int(b.sweep_counter.item()) == done
 
 
+@pytest.mark.parametrize("fmt", FORMATS)
 @pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("plan", [(136,), (20,), (20, 13, 1)])
 def test_headline_qubo1024_fold2_fused_bit_exact(oracle, schedule_knobs,
-                                                 plan, schedule):
+                                                 plan, schedule, fmt):
     """136 sweeps: a 128-sweep launch, then an 8-sweep one (fixed8: sixteen
     8-sweep units, then one; wrap2: three items over two CTAs, the middle
     item split at sweep 64, then at sweep 4).  20 and 20 + 13 + 1: runs
     whose length is not a multiple of 8, resumed across calls."""
     _run_vs_oracle(oracle, "qubo", 1024, 64, 3, 0.5, 8.0, plan, seed=11,
-                   fold=2, knobs=schedule_knobs, schedule=schedule)
+                   fold=2, knobs=schedule_knobs, schedule=schedule, fmt=fmt)
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
@@ -138,23 +145,27 @@ def test_headline_qubo1024_fold2_graph_replay_bit_exact(oracle, schedule_knobs,
                    fold=2, knobs=schedule_knobs, schedule=schedule)
 
 
-def test_headline_ising_pm1_fold2_fused_bit_exact(oracle):
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_headline_ising_pm1_fold2_fused_bit_exact(oracle, fmt):
     _run_vs_oracle(oracle, "ising", 1000, 64, 2, 0.3, 3.0, (136,), seed=13,
-                   fold=2)
+                   fold=2, fmt=fmt)
 
 
+@pytest.mark.parametrize("fmt", FORMATS)
 @pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("plan", [(136,), (20,)])
 def test_fold4_qubo1300_fused_bit_exact(oracle, schedule_knobs, plan,
-                                        schedule):
+                                        schedule, fmt):
     _run_vs_oracle(oracle, "qubo", 1300, 32, 3, 0.5, 8.0, plan, seed=14,
-                   fold=4, knobs=schedule_knobs, schedule=schedule)
+                   fold=4, knobs=schedule_knobs, schedule=schedule, fmt=fmt)
 
 
+@pytest.mark.parametrize("fmt", FORMATS)
 @pytest.mark.parametrize("schedule", SCHEDULES)
-def test_fold1_qubo512_fused_bit_exact(oracle, schedule_knobs, schedule):
+def test_fold1_qubo512_fused_bit_exact(oracle, schedule_knobs, schedule,
+                                       fmt):
     _run_vs_oracle(oracle, "qubo", 512, 32, 4, 0.5, 8.0, (136,), seed=15,
-                   fold=1, knobs=schedule_knobs, schedule=schedule)
+                   fold=1, knobs=schedule_knobs, schedule=schedule, fmt=fmt)
 
 
 def test_wrap_split_many_items_bit_exact(oracle, schedule_knobs):
