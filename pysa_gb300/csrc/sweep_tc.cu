@@ -1765,6 +1765,18 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
       if (lane == 0) {
         // rows [r_lo, r_hi) of the kTW-row B tile in `slot` against A slice
         // qq, into the field columns kTW j + r_lo ...
+        // Descriptors of the A region's and the B ring's starts, built once:
+        // a view or stage further in adds its byte offset / 16 to the
+        // address field (shared addresses stay below 2^18, so it never
+        // carries out).  The MMA thread shares its sub-partition with a
+        // deciding warp that is nearly always ready, and every instruction
+        // on its path waits for an issue slot, so it keeps few instructions
+        // per MMA (microbenchmark: a block's MMA sequence beside such a warp
+        // 10.3k cycles with descriptors built per call, 4.9k prebuilt).
+        const uint64_t a_desc0 =
+            tc::smem_desc(smem_base + (uint32_t)C::A_OFF, 128, C::SBO);
+        const uint64_t b_desc0 =
+            tc::smem_desc(smem_base + (uint32_t)C::B_OFF, 128, C::SBO);
         auto mma_rows = [&](uint32_t slot, int qq, int j, int r_lo, int r_hi,
                             uint32_t acc, int ab) {
           if (r_hi <= r_lo) return;
@@ -1773,19 +1785,16 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                   ? idesc_full
                   : (E8 ? tc::idesc_e4m3(128, r_hi - r_lo)
                         : tc::idesc_bf16(128, r_hi - r_lo));
-          // slice qq's view: 128 rows starting (128 - CC - qq CC) rows in
-          const uint32_t a0 =
-              smem_base +
-              (uint32_t)(C::A_OFF +
-                         (size_t)((128 - CC - qq * CC + 128 * ab) >> 3) * C::SBO);
-          const uint32_t b0 = smem_base +
-                              (uint32_t)(C::B_OFF + slot * C::B_STAGE) +
-                              (uint32_t)(r_lo / 8) * C::SBO;
+          // slice qq's view: 128 rows starting (128 - CC - qq CC) rows in;
           // K steps (16 BF16 or 32 E4M3 elements: two core matrices) are
-          // 256 bytes apart: 16 in the descriptors' address field (shared
-          // addresses stay below 2^18)
-          const uint64_t ad = tc::smem_desc(a0, 128, C::SBO);
-          const uint64_t bd = tc::smem_desc(b0, 128, C::SBO);
+          // 256 bytes apart: 16 in the address field
+          const uint64_t ad =
+              a_desc0 +
+              (uint64_t)((uint32_t)((128 - CC - qq * CC + 128 * ab) >> 3) *
+                         (C::SBO >> 4));
+          const uint64_t bd =
+              b_desc0 + (uint64_t)(slot * (uint32_t)(C::B_STAGE >> 4) +
+                                   (uint32_t)(r_lo / 8) * (C::SBO >> 4));
           if constexpr (E8) {
 #pragma unroll
             for (int ks = 0; ks < 2; ++ks)
