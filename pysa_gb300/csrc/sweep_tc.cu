@@ -856,7 +856,14 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
             // shuffle) and decide it identically; an accepted flip corrects
             // each lane's half of the fields.  The decisions, and every
             // rounding on their way, are those of the one-lane rounds below.
-            const int hf = lane >> 4, cc = 16 * warp + (lane & 15);
+            // Chains by groups of 8 (a quarter-warp's 16-byte accesses stay
+            // on distinct bank groups): warp w holds groups w and 7 - w, so
+            // replicas that start at neighbouring temperatures (and flip
+            // alike while the ladder has not mixed them) spread over the
+            // warps instead of loading one of them.
+            const int hf = lane >> 4;
+            const int cc =
+                8 * (((lane >> 3) & 1) ? 7 - warp : warp) + (lane & 7);
             bool ok = !*sh.abort;
             if (ok && q == qt && wait_h)
               ok = tc_wait(sh.h_ready, (Gb - 1) & 1, sh, status);
@@ -945,29 +952,40 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                 const uint32_t c0 = hf ? other : cand, c1 = hf ? cand : other;
                 if (L == 0) count(a, 2, 1);
                 if (__all_sync(0xffffffffu, (c0 | c1) == 0u)) break;
+                // the chain's next decision (positions up to it decided)
+                const int js = c0 ? __ffs(c0) - 1
+                                  : (c1 ? 32 + __ffs(c1) - 1 : 0);
+                // its field at decision: the lane holding position js has it
+                // in registers, corrected by this block's earlier flips in
+                // position order (the values and roundings of a rebuild from
+                // the loaded fields); a select tree picks it and the partner
+                // takes it by shuffle, in every lane so the warp stays
+                // converged
+                float hsel;
+                {
+                  const int jl = js & 31;
+                  float v16[16], v8[8], v4[4], v2[2];
+#pragma unroll
+                  for (int i = 0; i < 16; ++i) v16[i] = (jl & 16) ? h[i + 16] : h[i];
+#pragma unroll
+                  for (int i = 0; i < 8; ++i) v8[i] = (jl & 8) ? v16[i + 8] : v16[i];
+#pragma unroll
+                  for (int i = 0; i < 4; ++i) v4[i] = (jl & 4) ? v8[i + 4] : v8[i];
+#pragma unroll
+                  for (int i = 0; i < 2; ++i) v2[i] = (jl & 2) ? v4[i + 2] : v4[i];
+                  hsel = (jl & 1) ? v2[1] : v2[0];
+                }
+                const float hpart = __shfl_xor_sync(0xffffffffu, hsel, 16);
                 if ((c0 | c1) == 0u) {
                   pend = 0u;  // the rest rejected: done
                 } else {
-                  // the chain's next decision; positions up to it decided
-                  int js;
                   if (c0) {
-                    js = __ffs(c0) - 1;
                     if (hf == 0) pend &= ~((2u << js) - 1u);
                   } else {
-                    js = 32 + __ffs(c1) - 1;
                     pend = hf == 0 ? 0u : pend & ~((2u << (js - 32)) - 1u);
                   }
                   const uint64_t bit = 1ull << js;
-                  // the field at decision: loaded value + this block's
-                  // earlier flips, in the order the fields took them
-                  float hj = dl_s[cidx(cc, js)];
-                  uint64_t fb = flips64;
-                  while (fb) {
-                    const int i = __ffsll((long long)fb) - 1;
-                    fb &= fb - 1ull;
-                    const uint32_t si = (i < 32 ? o0 >> i : o1 >> (i - 32)) & 1u;
-                    hj = fmaf(si ? -scale : scale, jb[i * 64 + js], hj);
-                  }
+                  const float hj = (js >> 5) == hf ? hsel : hpart;
                   const bool sbit =
                       ((js < 32 ? o0 >> js : o1 >> (js - 32)) & 1u) != 0u;
                   const float x = sbit ? hj : -hj;
