@@ -933,7 +933,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               for (;;) {
                 const uint32_t lo = __reduce_min_sync(
                     0xffffffffu, pend ? (uint32_t)(__ffs(pend) - 1) : 32u);
-                uint32_t m[4];  // bit k: position certainly rejected
+                // bit k: the sign of h + w at position k.  A position is
+                // certainly rejected when h + w and w differ in sign -- the
+                // sign of their product, zeros and infinities included, as
+                // the one-lane rounds test it -- and w is negative exactly
+                // where the spin is 0 (w = -|tl|, tl = a / (beta scale) < 0),
+                // so the candidates are (signs ^ spins) & undecided
+                uint32_t m[4];
 #pragma unroll
                 for (int qd = 0; qd < 4; ++qd) {
                   m[qd] = 0u;
@@ -941,13 +947,14 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
 #pragma unroll
                     for (int jj = 7; jj >= 0; --jj) {
                       const int k = 8 * qd + jj;
-                      const uint32_t x = __float_as_uint((h[k] + w[k]) * w[k]);
-                      m[qd] = __funnelshift_l(x, m[qd], 1);
+                      m[qd] = __funnelshift_l(__float_as_uint(h[k] + w[k]),
+                                              m[qd], 1);
                     }
                   }
                 }
                 const uint32_t cand =
-                    ~(m[0] | (m[1] << 8) | (m[2] << 16) | (m[3] << 24)) & pend;
+                    ((m[0] | (m[1] << 8) | (m[2] << 16) | (m[3] << 24)) ^ om) &
+                    pend;
                 const uint32_t other = __shfl_xor_sync(0xffffffffu, cand, 16);
                 const uint32_t c0 = hf ? other : cand, c1 = hf ? cand : other;
                 if (L == 0) count(a, 2, 1);
