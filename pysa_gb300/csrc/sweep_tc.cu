@@ -97,7 +97,9 @@ struct TcCfg {
   // F == 2, visiting order: block rounds run on all four decision warps,
   // two lanes per chain (the other slice's warps would idle)
   static constexpr bool PAIRS = F == 2 && !RND;
-  static constexpr size_t CORR_OFF = BETA_OFF + CC * 4;
+  // 1 / (beta scale) of each chain (+inf for beta <= 0), kept with beta_s
+  static constexpr size_t INVB_OFF = BETA_OFF + CC * 4;
+  static constexpr size_t CORR_OFF = INVB_OFF + CC * 4;
   static constexpr size_t CORR_BYTES = HELP ? (size_t)2 * 16 * CC * 4 : 0;
   // RND, F > 1: fields of the block's 64 scattered columns, gathered by the
   // warps whose slices hold them ([64][CC] floats)
@@ -451,6 +453,13 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   double* e0_s = reinterpret_cast<double*>(smem + C::E0_OFF);
   double* epart_s = reinterpret_cast<double*>(smem + C::EPART_OFF);
   float* beta_s = reinterpret_cast<float*>(smem + C::BETA_OFF);
+  float* invb_s = reinterpret_cast<float*>(smem + C::INVB_OFF);
+  // the field-unit scale of a chain's rejection threshold: 1 / (beta scale)
+  auto inv_bs = [&](float b) {
+    return b > 0.0f ? 1.0f / (b * (a.p.problem_type == PYSA_GB_ISING ? 2.0f
+                                                                     : 1.0f))
+                    : INFINITY;
+  };
   const float* jbb = reinterpret_cast<const float*>(smem + C::JBB_OFF);
   float* lf_s = reinterpret_cast<float*>(smem + C::LF_OFF);
   float* dl_s = reinterpret_cast<float*>(smem + C::DL_OFF);
@@ -619,6 +628,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
                      : 0.0;
       beta_s[cc] =
           cc < item.nchains ? __ldcg(a.s.chain_beta + item.chain0 + cc) : 0.0f;
+      invb_s[cc] = inv_bs(beta_s[cc]);
     }
     if (threadIdx.x == 0) stamp_cta(a, 5);
     if (warp < 4 && !rc_at(0)) {  // local fields -> TMEM
@@ -894,8 +904,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               const uint32_t om = hf ? o1 : o0;  // this lane's half
               const float pbeta = beta_s[cc];
               const float scale = ising ? 2.0f : 1.0f;
-              const float invbs =
-                  pbeta > 0.0f ? 1.0f / (pbeta * scale) : INFINITY;
+              const float invbs = invb_s[cc];  // 1 / (pbeta scale), or +inf
               const bool banded = pvalid && invbs < INFINITY;
               const float band0 = banded ? 3e-5f * invbs : 0.0f;
               const float band1 = banded ? 1e-6f * invbs : 0.0f;
@@ -1737,6 +1746,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
               a.s.beta_idx[gbase + k] = B[k];
               a.s.chain_beta[gbase + B[k]] = Bt[k];
               beta_s[r * R + B[k]] = Bt[k];
+              invb_s[r * R + B[k]] = inv_bs(Bt[k]);
             }
             __syncwarp();
           }
