@@ -305,6 +305,15 @@ int pysa_gb_set_block_round_limit(int32_t flips);
  * launches enqueued after the call.  No counterpart in the reference. */
 int pysa_gb_set_tc_max_ctas(int32_t ctas);
 
+/* The tensor-core sweep's wrap-around schedule, as the kernel computes it
+ * (host copy of the same code, for tests and tools): piece `piece` of share
+ * `share` when `ctas` CTAs split `items` work items x `sweeps` sweeps of a
+ * launch (ctas <= items).  Returns 1 and out = {item, first sweep, sweeps},
+ * 0 past the share's last piece, or an error.  No counterpart in the
+ * reference. */
+int pysa_gb_tc_wrap_piece(int32_t items, int32_t sweeps, int32_t ctas,
+                          int32_t share, int32_t piece, int32_t out[3]);
+
 /* Workspace sizing and set-up.
  *   pysa_gb_workspace_bytes: sizes of the workspace arrays for a batch
  *     described by host tables (n, replicas, reads are read); returns the

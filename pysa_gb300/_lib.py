@@ -113,6 +113,7 @@ def load() -> ctypes.CDLL:
         "pysa_gb_set_decision_mode": ([ctypes.c_int32], ctypes.c_int),
         "pysa_gb_set_block_round_limit": ([ctypes.c_int32], ctypes.c_int),
         "pysa_gb_set_tc_max_ctas": ([ctypes.c_int32], ctypes.c_int),
+        "pysa_gb_tc_wrap_piece": ([ctypes.c_int32] * 5 + [P], ctypes.c_int),
         "pysa_gb_last_error": ([], ctypes.c_char_p),
         "pysa_gb_workspace_bytes": ([I32, P, P], ctypes.c_int),
         "pysa_gb_setup": ([P, P, P, P], ctypes.c_int),

@@ -159,6 +159,19 @@ int pysa_gb_set_tc_max_ctas(int32_t ctas) {
   return PYSA_GB_OK;
 }
 
+int pysa_gb_tc_wrap_piece(int32_t items, int32_t sweeps, int32_t ctas,
+                          int32_t share, int32_t piece, int32_t out[3]) {
+  if (!out || items < 1 || sweeps < 1 || ctas < 1 || ctas > items ||
+      share < 0 || share >= ctas || piece < 0)
+    return fail(PYSA_GB_ERR_ARG, "wrap piece: bad arguments");
+  int it = -1, sb = 0, sl = 0;
+  if (!wrap_piece(items, sweeps, ctas, share, piece, &it, &sb, &sl)) return 0;
+  out[0] = it;
+  out[1] = sb;
+  out[2] = sl;
+  return 1;
+}
+
 int pysa_gb_set_trace(void* device_buffer) {
   g_tc_trace = reinterpret_cast<unsigned long long*>(device_buffer);
   return PYSA_GB_OK;

@@ -55,6 +55,46 @@ struct TcArgs {
   unsigned long long* trace;
 };
 
+// Wrap-around split of a launch's num_items * S item-sweeps over m CTAs
+// (McNaughton's rule for preemptive scheduling on identical machines): share
+// k holds positions [k T / m, (k + 1) T / m) of the item-major order (sweep s
+// of item i at i S + s, T = num_items S), and num_items >= m makes every
+// share at least S long.  Its pieces, in order: the head of the item the
+// share ends in (sweeps 0 .. p1 % S - 1), its whole items, then the tail of
+// the item it starts in (sweeps p0 % S .. S - 1).  That tail's head is the
+// first piece of share k - 1 and, with sweeps of equal cost, is done before
+// the tail starts.  Piece j of share k -> (item, first sweep, sweeps);
+// false past the last piece.
+__host__ __device__ inline bool wrap_piece(int items, int S, int m, int k,
+                                           int j, int* it, int* sb, int* sl) {
+  const int64_t T = (int64_t)items * S;
+  const int64_t p0 = T * k / m, p1 = T * (k + 1) / m;
+  const int head = (int)(p1 % S), tail = (int)(p0 % S);
+  const int64_t f0 = (p0 + S - 1) / S, f1 = p1 / S;  // whole items [f0, f1)
+  if (head) {
+    if (j == 0) {
+      *it = (int)(p1 / S);
+      *sb = 0;
+      *sl = head;
+      return true;
+    }
+    --j;
+  }
+  if (j < f1 - f0) {
+    *it = (int)(f0 + j);
+    *sb = 0;
+    *sl = S;
+    return true;
+  }
+  if (tail && j == f1 - f0) {
+    *it = (int)(p0 / S);
+    *sb = tail;
+    *sl = S - tail;
+    return true;
+  }
+  return false;
+}
+
 int tc_fold_for(int n);  // 1, 2, 4 or -1 (n > 2048)
 int tc_chains_per_cta(int n);
 int64_t tc_b_elems(int n, int terms);

@@ -113,6 +113,74 @@ def test_schedule_knobs_validate_without_gpu():
     assert lib.pysa_gb_set_tc_max_ctas(0) == 0
 
 
+def _wrap_plan(lib, items, sweeps, ctas):
+    out = (ctypes.c_int32 * 3)()
+    plan = []
+    for k in range(ctas):
+        pieces = []
+        j = 0
+        while True:
+            r = lib.pysa_gb_tc_wrap_piece(items, sweeps, ctas, k, j, out)
+            assert r in (0, 1)
+            if r == 0:
+                break
+            pieces.append((out[0], out[1], out[2]))
+            j += 1
+        plan.append(pieces)
+    return plan
+
+
+@pytest.mark.parametrize("items,sweeps,ctas", [
+    (256, 20, 152), (256, 128, 152), (3, 136, 2), (7, 128, 3), (7, 9, 3),
+    (5, 1, 5), (152, 5, 152), (1000, 13, 152), (153, 128, 152), (2, 7, 1)])
+def test_wrap_schedule_covers_every_item_sweep_in_order(items, sweeps, ctas):
+    """The kernel's wrap-around split (host copy of the same code): every
+    (item, sweep) is run exactly once; each CTA runs at most one head (the
+    first sweeps of an item, first) and one tail (the last sweeps of an
+    item, last) around whole items; the CTA holding a tail is the next one
+    after the CTA holding that item's head, whose head is its first piece
+    and ends, at one time unit per item-sweep, no later than the tail
+    starts; shares differ by at most one item-sweep."""
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    plan = _wrap_plan(lib, items, sweeps, ctas)
+    seen = np.zeros((items, sweeps), np.int32)
+    where = {}
+    for k, pieces in enumerate(plan):
+        t = 0
+        for j, (it, sb, sl) in enumerate(pieces):
+            assert 0 <= it < items and sl >= 1 and sb + sl <= sweeps
+            seen[it, sb:sb + sl] += 1
+            where.setdefault(it, []).append((sb, sl, k, j, t))
+            if sb > 0:
+                assert j == len(pieces) - 1, "a tail runs last"
+            if sl < sweeps and sb == 0:
+                assert j == 0, "a head runs first"
+            t += sl
+    assert (seen == 1).all()
+    sizes = [sum(p[2] for p in pieces) for pieces in plan]
+    assert max(sizes) - min(sizes) <= 1
+    for it, parts in where.items():
+        parts.sort()
+        if len(parts) == 1:
+            assert parts[0][:2] == (0, sweeps)
+            continue
+        assert len(parts) == 2
+        (hb, hl, hk, hj, ht), (tb, tl, tk, tj, tt) = parts
+        assert hb == 0 and tb == hl and tb + tl == sweeps
+        assert tk == hk + 1 and hj == 0
+        assert ht + hl <= tt, "the head ends before the tail starts"
+
+
+def test_wrap_schedule_rejects_bad_arguments():
+    from pysa_gb300 import _lib
+    lib = _lib.load()
+    out = (ctypes.c_int32 * 3)()
+    assert lib.pysa_gb_tc_wrap_piece(3, 10, 4, 0, 0, out) == -1  # ctas > items
+    assert lib.pysa_gb_tc_wrap_piece(4, 10, 4, 4, 0, out) == -1  # share out
+    assert lib.pysa_gb_tc_wrap_piece(4, 0, 4, 0, 0, out) == -1
+
+
 def test_e4m3_exactness_matches_torch_conversion():
     """The host check that selects FP8 E4M3 tiles agrees with a round trip
     through torch's float8_e4m3fn on integers, subnormals, the largest
