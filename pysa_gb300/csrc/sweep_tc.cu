@@ -10,12 +10,14 @@
 //   * for a block of 64 spins each chain's thread reads its 64 fields
 //     (tcgen05.ld), decides the 64 spins one after another, applying the exact
 //     in-block field corrections from the FP32 64x64 diagonal block of J, and
-//     writes its flips delta in {0, +-1, +-2} (exact in BF16) into the A tile;
+//     writes its flips delta in {0, +-1, +-2} (exact in BF16 and E4M3) into
+//     the A tile;
 //   * one thread issues the cross-block update H += A * B as tcgen05.mma with
 //     B = J rows of the block split as J_hi + J_lo in BF16 (one term when J is
-//     exactly BF16), FP32 accumulation in TMEM.  The MMA of the tile holding
-//     the next block's columns is committed first so the next decisions start
-//     while the remaining tiles run.
+//     exactly BF16; optionally one E4M3 term when J is exactly E4M3, the
+//     E8 variants in sweep_tc_e8.cu), FP32 accumulation in TMEM.  The MMA of
+//     the tile holding the next block's columns is committed first so the
+//     next decisions start while the remaining tiles run.
 // B tiles (pre-laid-out in the canonical no-swizzle K-major core-matrix order)
 // and the diagonal blocks stream in through a ring of shared-memory stages by
 // 1-D bulk copies (TMA engine).  Integer couplings make every product and sum
@@ -24,8 +26,10 @@
 // Roles: warps 0-3 decide (thread = TMEM lane; with F > 1 only the warps of
 // the slice holding the block's columns, the others help: at F = 2 they
 // compute the older sub-blocks' corrections and write A rows, at F = 4 they
-// write A rows), warp 4 issues MMAs, warp 5 produces stages, warps 6-7
-// precompute the next block's log-uniforms.  Every wait is bounded; a
+// write A rows; in block rounds at F = 2 all four decide, two lanes per
+// chain, from fields the holding slice stashes in shared memory), warp 4
+// issues MMAs, warp 5 produces stages, warps 6-7 precompute the next
+// block's log-uniforms.  Every wait is bounded; a
 // timeout sets the status word and an abort flag that releases every other
 // wait.
 #include <cuda_fp8.h>
