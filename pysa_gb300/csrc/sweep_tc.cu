@@ -449,19 +449,18 @@ __global__ void __launch_bounds__(256, 1) k_sweep_tc(const TcArgs a) {
   auto a_row = [&](int m) {
     return smem + C::A_OFF + ((m >> 3) * C::CPR) * 128 + (m & 7) * 16;
   };
-  const bool ising_ = a.p.problem_type == PYSA_GB_ISING;
+  const bool ising = a.p.problem_type == PYSA_GB_ISING;
   auto a_put = [&](unsigned char* rowp, int j, bool neg) {
     if constexpr (E8)
       rowp[(j >> 4) * 128 + (j & 15)] =
-          (unsigned char)((ising_ ? 0x40u : 0x38u) | (neg ? 0x80u : 0u));
+          (unsigned char)((ising ? 0x40u : 0x38u) | (neg ? 0x80u : 0u));
     else
       *reinterpret_cast<uint16_t*>(rowp + (j >> 3) * 128 + (j & 7) * 2) =
-          (uint16_t)((ising_ ? 0x4000u : 0x3F80u) | (neg ? 0x8000u : 0u));
+          (uint16_t)((ising ? 0x4000u : 0x3F80u) | (neg ? 0x8000u : 0u));
   };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int32_t* status = a.s.status;
-  const bool ising = a.p.problem_type == PYSA_GB_ISING;
   const uint32_t sweep0 = (uint32_t)(*a.s.sweep_counter);
   const int total_units = a.num_items * a.units_per_item;
   const int T = a.terms;
