@@ -583,7 +583,9 @@ class PTBatch:
         n = int(self.n[0]) if len(self.n) else 0
         if len(self.n) and (self.n != n).any():
             raise ValueError("set_states_device needs one n for the batch")
-        x = states.detach().to(device=self.device, dtype=torch.float32)
+        # to the device in the caller's dtype (int8 states move a quarter of
+        # float32's bytes), float32 there
+        x = states.detach().to(device=self.device).to(torch.float32)
         x = x.reshape(self.num_chains, n).contiguous()
         st = self._stream.cuda_stream
         check(self.lib.pysa_gb_pack(self.ptype, n, _ptr(x), n,

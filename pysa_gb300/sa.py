@@ -236,16 +236,23 @@ class Solver(object):
 
         # initial states, pysa/sa.py:214-313 (NumPy global RNG, per read)
         energies_given = None
+        draw_small = None  # random: the read's values as small integers
         if type(initialize_strategy) == str:
             if initialize_strategy == 'random':
                 if self.problem_type == 'qubo':
                     def draw():
                         return np.random.randint(2, size=(R, N)).astype(
                             self.float_type)
+
+                    def draw_small():
+                        return np.random.randint(2, size=(R, N))
                 elif self.problem_type == 'ising':
                     def draw():
                         return 2 * np.random.randint(2, size=(R, N)).astype(
                             self.float_type) - 1
+
+                    def draw_small():
+                        return 2 * np.random.randint(2, size=(R, N)) - 1
                 else:
                     raise ValueError(
                         f"self.problem_type=='{self.problem_type}' not supported.")
@@ -293,8 +300,18 @@ class Solver(object):
         # ------------------------------------------------- GPU run
         t0 = time()
         Rd = int(num_reads)
-        states0 = np.stack([draw() for _ in range(Rd)]) if Rd else np.zeros(
-            (0, R, N), self.float_type)
+        if Rd and draw_small is not None:
+            # the same NumPy RNG calls, read after read, with the values
+            # (0/1 or +-1) written straight into one int8 array: no float
+            # copies on the host and a quarter of the bytes to the device,
+            # where they become float32 exactly
+            states0 = np.empty((Rd, R, N), np.int8)
+            for r in range(Rd):
+                states0[r] = draw_small()
+        elif Rd:
+            states0 = np.stack([draw() for _ in range(Rd)])
+        else:
+            states0 = np.zeros((0, R, N), self.float_type)
         batch = PTBatch(self.problem_type, [
             Instance(np.asarray(couplings, np.float32),
                      np.asarray(local_fields, np.float32),
@@ -308,7 +325,9 @@ class Solver(object):
             import torch
             batch.set_states_device(
                 torch.from_numpy(np.ascontiguousarray(
-                    states0.reshape(Rd * R, N), dtype=np.float32)),
+                    states0.reshape(Rd * R, N),
+                    dtype=np.int8 if states0.dtype == np.int8
+                    else np.float32)),
                 None if e0 is None else torch.from_numpy(e0),
                 best_global=not parallel)
         else:
