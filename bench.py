@@ -1288,10 +1288,10 @@ def main():
         rows = solver.metropolis_update(**kw, seed=2)
         e2e_s = time.perf_counter() - t0
         words = batch.words
-        # couplings, fields, ladder, float32 states (packed on the device);
-        # float32 final states, spin words of the best states, per-chain
-        # energies, slots, best energies and sweeps
-        h2d = 4 * n * n + 4 * n + 4 * R + C * n * 4
+        # couplings, fields, ladder, int8 initial states (made float32 and
+        # packed on the device); float32 final states, spin words of the
+        # best states, per-chain energies, slots, best energies and sweeps
+        h2d = 4 * n * n + 4 * n + 4 * R + C * n
         d2h = C * (n * 4 + words * 4 * 2 + 4 * 4)
         # the returned energies must be the energies of the returned states
         # (f64 recomputation, pysa/qubo.py:32-37; exact for integer QUBO)
